@@ -1,0 +1,374 @@
+#!/usr/bin/env python
+"""Benchmark of the GCOO sparse x dense multiply on GB300.
+
+Workload: A 8192 x 8192 FP32 with a Bernoulli(0.01) nonzero mask (sparsity
+0.99) and U(-1,1) values, B 8192 x 8192 FP32 U(-1,1), seeded synthetic data.
+One step = one mutiplyBy (dense -> GCOO conversion + FP32 multiply), the
+measure the reference publishes. value = 2 * nnz * n / step time (GFLOP/s),
+summed over ranks (each rank runs its own replica: the path needs no
+exchange between GPUs).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU restatement (the oracle
+port; the reference itself has no CPU implementation of this path) on the
+host cores, on a bounded row sample of the same workload.
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 8192
+METRIC = "SpDM GFLOP/s (2*nnz*n), dense->GCOO conversion + FP32 multiply per step"
+UNIT = "GFLOP/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=8192, help="m = k = n of the square workload")
+    ap.add_argument("--sparsity", type=float, default=0.99)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the extra precision/batched lines")
+    return ap.parse_args()
+
+
+def dist_setup(gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+                "sm_max_mhz": 2070.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return None
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    rows.append((float(p[1]), float(p[2]), p[5:9], float(p[3]) if p[3] not in ("[N/A]", "") else 0.0))
+                except ValueError:
+                    continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[2]) if v.lower() == "active"})
+        loaded = [r for r in rows if r[3] > 200.0] or rows
+        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_sample_gflops(A_rows, B, cpg=4, target_s=1.0):
+    """Oracle port (convert + multiply) on a row sample, all host threads."""
+    import numpy as np
+    import oracle
+    nt = oracle.max_threads() or os.cpu_count() or 1
+    rows = A_rows
+    nnz = int(np.count_nonzero(rows))
+    n = B.shape[1]
+    oracle.multiply_by(rows[: min(64, rows.shape[0])], B, cpg, nt)  # warm the pages
+    times = []
+    t_end = time.perf_counter() + target_s
+    while len(times) < 3 or (time.perf_counter() < t_end and len(times) < 20):
+        t0 = time.perf_counter()
+        oracle.multiply_by(rows, B, cpg, nt)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    return 2.0 * nnz * n / t / 1e9, nt, len(times), t
+
+
+def run_reference(args, rank, world):
+    """The reference algorithm's CPU implementation (oracle port), host cores."""
+    if rank != 0:
+        return
+    import numpy as np
+    from gcoospdm_gb300 import datagen as dg
+    import oracle
+    oracle.build()
+    n = args.n
+    p = 1.0 - args.sparsity
+    B = dg.dense_pm1(SEED, 5, n, n)
+    probe = dg.bernoulli_dense(SEED, 256, n, p)
+    g, nt, _, t = cpu_sample_gflops(probe, B, target_s=0.2)
+    rows = int(max(256, min(n, 256 * 0.5 / max(t, 1e-6)))) // 4 * 4  # ~0.5 s per step
+    A = dg.bernoulli_dense(SEED, rows, n, p)
+    nnz = int(np.count_nonzero(A))
+    for _ in range(args.warmup):
+        oracle.multiply_by(A, B, 4, nt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.multiply_by(A, B, 4, nt)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = 2.0 * nnz * n / dt / 1e9
+    sample = f"rows 0..{rows} of the {n}x{n} s={args.sparsity} matrix (convert + multiply), B {n}x{n}"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded splitmix64)",
+        "config": {"workload": f"fp32 gcoo convert+multiply, A {n}x{n} bernoulli p={p:g} U(-1,1), B {n}x{n} U(-1,1)",
+                   "m": n, "k": n, "n": n, "sparsity": args.sparsity, "rows_per_group": 4,
+                   "l2": "host run (no GPU)"},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": nt, "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference has no CPU implementation of this path; the oracle restates its algorithm "
+                "(src/gcoo_spdm_kernels.cu) in C with OpenMP",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def load_profile_traffic():
+    p = os.path.join(ROOT, "profiles", "spdm_fp32_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except OSError:
+        return None
+
+
+def run_ours(args, rank, world, local, pg):
+    import torch
+    import gcoospdm_gb300 as g
+    from gcoospdm_gb300 import datagen as dg
+
+    if not os.path.exists(g.LIB_PATH):
+        g.build()
+    torch.cuda.set_device(local)
+    L = g.lib()
+    n = args.n
+    m = k = n
+    p = 1.0 - args.sparsity
+    dev = torch.device("cuda", local)
+    A = dg.bernoulli_dense_torch(SEED, m, k, p, device=dev)
+    B = dg.dense_pm1_torch(SEED, 5, k, n, device=dev)
+    Cd = torch.empty(m, n, device=dev)
+    h = g.GcooHandle(A).build()
+    nnz = h.nnz
+    flop = 2.0 * nnz * n
+    stream = torch.cuda.current_stream()
+
+    # ---- headline: convert + multiply per step, device-resident inputs -------------
+    for _ in range(args.warmup):
+        h.multiply_by(B, Cd)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(pg)
+    torch.cuda.synchronize()
+    launches0 = L.gcoo_kernel_launches()
+    with Clocks(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            h.multiply_by(B, Cd)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = L.gcoo_kernel_launches() - launches0
+    barrier(pg)
+    ms = max_over_ranks(pg, e0.elapsed_time(e1) / args.steps)
+    value = flop * world / (ms * 1e-3) / 1e9
+    clocks = clk.summary()
+
+    # ---- the dominant kernel alone (multiply only), for the roofline --------------
+    reps = max(args.steps, 10)
+    for _ in range(3):
+        h.spdm(B, Cd)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        h.spdm(B, Cd)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_spdm = e0.elapsed_time(e1) / reps * 1e-3
+    ng = (m + 3) // 4
+    alg_bytes = 12 * nnz + 8 * (ng + 1) + 4 * k * n + 4 * m * n
+    peaks, peak_kind = measured_peaks()
+    achieved = alg_bytes / t_spdm / 1e9
+    prof = load_profile_traffic()
+    traffic = None
+    if prof and prof.get("n") == n and abs(prof.get("sparsity", 0) - args.sparsity) < 1e-9:
+        traffic = prof.get("dram_bytes_per_launch")
+    fma_peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    # conversion alone (build: count + scan + scatter, one readback)
+    for _ in range(2):
+        h.build()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(5):
+        h.build()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_conv = e0.elapsed_time(e1) / 5 * 1e-3
+    err = h.error_norm(B, Cd)
+
+    # ---- end to end through the C ABI with host buffers ------------------------------
+    e2e = None
+    if not args.no_e2e:
+        Ah = A.cpu().pin_memory()
+        Bh = B.cpu().pin_memory()
+        Ch = torch.empty(m, n, dtype=torch.float32).pin_memory()
+        Ad = torch.empty_like(A)
+        Bd = torch.empty_like(B)
+        h2 = g.GcooHandle(Ad)
+
+        def e2e_step():
+            Ad.copy_(Ah, non_blocking=True)
+            Bd.copy_(Bh, non_blocking=True)
+            h2.multiply_by(Bd, Cd)
+            Ch.copy_(Cd, non_blocking=True)
+
+        for _ in range(args.warmup):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(pg)
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_e2e = max_over_ranks(pg, e0.elapsed_time(e1) / args.steps)
+        e2e = {"value": round(flop * world / (ms_e2e * 1e-3) / 1e9, 3), "unit": UNIT,
+               "h2d_bytes_per_step": int(Ah.numel() * 4 + Bh.numel() * 4), "d2h_bytes_per_step": int(Ch.numel() * 4),
+               "ms_per_step": round(ms_e2e, 4)}
+        assert torch.equal(Ch.to(dev), Cd)
+        del h2
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import numpy as np
+        rows = 512
+        Ah_rows = A[:rows].cpu().numpy()
+        Bh_np = B.cpu().numpy()
+        gfl, nt, nrep, t = cpu_sample_gflops(np.ascontiguousarray(Ah_rows), np.ascontiguousarray(Bh_np), target_s=3.0)
+        cpu = {"value": round(gfl, 3), "unit": UNIT, "cores": nt, "kind": "port",
+               "sample": f"rows 0..{rows} of A (convert + multiply) x full B, median of {nrep} runs ({t:.3f} s each)"}
+
+    forms = None
+    if not args.no_forms:
+        forms = run_forms(args, g, dg, torch, dev)
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": round(value / 117.1, 3) if (n == 8192 and abs(args.sparsity - 0.99) < 1e-9) else None,
+        "dtype": "f32", "data": "synthetic (seeded splitmix64; U(-1,1) values, Bernoulli mask)",
+        "config": {"workload": f"fp32 gcoo convert+multiply, A {m}x{k} bernoulli p={p:g} U(-1,1), B {k}x{n} U(-1,1)",
+                   "m": m, "k": k, "n": n, "sparsity": args.sparsity, "nnz": nnz, "rows_per_group": 4,
+                   "l2": "no flush: inputs larger than L2 (A and B 268 MB each, L2 129 MB)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
+                     "kernel": "spdm_fp32_kernel", "algorithmic_bytes": alg_bytes,
+                     "kernel_ms": round(t_spdm * 1e3, 4), "peak_source": peak_kind},
+        "fma_roofline": {"achieved_tflops": round(flop / t_spdm / 1e12, 3), "nominal_peak_tflops": round(fma_peak, 1),
+                         "frac": round(flop / t_spdm / 1e12 / fma_peak, 4)},
+        "spdm_only_gflops": round(flop / t_spdm / 1e9, 3),
+        "convert_ms": round(t_conv * 1e3, 4),
+        "rel_fro_vs_fp64": err,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    if forms:
+        line["forms"] = forms
+    print(json.dumps(line), flush=True)
+
+
+def run_forms(args, g, dg, torch, dev):
+    """Extra measurements of the other arithmetic forms (filled as they land)."""
+    return None
+
+
+def main():
+    args = parse()
+    rank, world, local, pg = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,426 @@
+// api.cu -- the C ABI (include/gcoo.h): validation, handle lifecycle, the
+// conversion orchestration and dispatch to the kernels. Every entry point
+// returns a status; CUDA errors are captured after each launch.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <atomic>
+#include <mutex>
+#include <string>
+
+#include "handle.hpp"
+
+namespace gcoo {
+
+// ---- errors --------------------------------------------------------------------
+static thread_local std::string t_last_error;
+
+void set_error(const std::string &msg) { t_last_error = msg; }
+
+gcoo_status fail(gcoo_status s, const std::string &msg)
+{
+    t_last_error = std::string(gcoo_status_string(s)) + ": " + msg;
+    return s;
+}
+
+gcoo_status cuda_fail(cudaError_t e, const char *what)
+{
+    t_last_error = std::string("CUDA error in ") + what + ": " + cudaGetErrorName(e) + " (" +
+                   cudaGetErrorString(e) + ")";
+    return e == cudaErrorMemoryAllocation ? GCOO_ERROR_ALLOC : GCOO_ERROR_CUDA;
+}
+
+// ---- launch counter ------------------------------------------------------------------
+static std::atomic<uint64_t> g_launches{0};
+void count_launches(int n) { g_launches.fetch_add(static_cast<uint64_t>(n), std::memory_order_relaxed); }
+
+// ---- allocator ---------------------------------------------------------------------
+static gcoo_alloc_fn g_alloc = nullptr;
+static gcoo_free_fn g_free = nullptr;
+static void *g_alloc_ctx = nullptr;
+
+void *dev_alloc(size_t bytes)
+{
+    if (g_alloc)
+        return g_alloc(bytes, g_alloc_ctx);
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+        cudaGetLastError(); // clear the sticky-free error state of this call
+        return nullptr;
+    }
+    return p;
+}
+
+void dev_free(void *p)
+{
+    if (!p)
+        return;
+    if (g_free)
+        g_free(p, g_alloc_ctx);
+    else
+        cudaFree(p);
+}
+
+// Implemented in forms.cu / autotune.cpp.
+gcoo_status run_form(gcoo_handle *h, const float *dB, int64_t n, float *dC, gcoo_precision prec,
+                     cudaStream_t st, bool prepare_only);
+bool form_uses_tensor(gcoo_handle *h, gcoo_precision prec);
+bool tuned_params(int64_t m, int64_t k, int64_t nnz, int64_t n, gcoo_params *out);
+
+static bool valid_cpg(int32_t c) { return c == 1 || c == 2 || c == 4 || c == 8 || c == 16 || c == 32; }
+
+static gcoo_status check_dims(int64_t m, int64_t k)
+{
+    if (m <= 0 || k <= 0)
+        return fail(GCOO_ERROR_INVALID_VALUE, "m and k must be positive");
+    if (m >= (int64_t(1) << 31) || k >= (int64_t(1) << 31))
+        return fail(GCOO_ERROR_INVALID_VALUE, "m and k must fit int32 indices");
+    return GCOO_SUCCESS;
+}
+
+static gcoo_status check_n(int64_t n)
+{
+    if (n <= 0 || n >= (int64_t(1) << 31))
+        return fail(GCOO_ERROR_INVALID_VALUE, "n must be in [1, 2^31)");
+    return GCOO_SUCCESS;
+}
+
+gcoo_status spdm_fp32(gcoo_handle *h, const float *dB, int64_t n, float *dC, cudaStream_t st,
+                      const gcoo_params *override_params)
+{
+    gcoo_params p = h->p;
+    if (override_params) {
+        p = *override_params;
+        p.rows_per_group = h->p.rows_per_group;
+    } else {
+        gcoo_params t;
+        if (tuned_params(h->m, h->k, h->nnz, n, &t)) {
+            p.vec = t.vec;
+            p.warps = t.warps;
+            p.col_warps = t.col_warps;
+        }
+    }
+    const LaunchShape s = pick_shape(p, h->m, n, h->nnz, reinterpret_cast<uintptr_t>(dB),
+                                     reinterpret_cast<uintptr_t>(dC));
+    cudaError_t e = launch_spdm_fp32(h->packed.ptr, h->row_ptr.ptr, h->m, h->p.rows_per_group, dB, n, dC, s,
+                                     h->status.ptr, st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "spdm_fp32_kernel launch");
+    return GCOO_SUCCESS;
+}
+
+} // namespace gcoo
+
+using namespace gcoo;
+
+extern "C" {
+
+int gcoo_abi_version(void) { return GCOO_ABI_VERSION; }
+
+uint64_t gcoo_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+const char *gcoo_status_string(gcoo_status s)
+{
+    switch (s) {
+    case GCOO_SUCCESS: return "GCOO_SUCCESS";
+    case GCOO_ERROR_INVALID_VALUE: return "GCOO_ERROR_INVALID_VALUE";
+    case GCOO_ERROR_ALLOC: return "GCOO_ERROR_ALLOC";
+    case GCOO_ERROR_CUDA: return "GCOO_ERROR_CUDA";
+    case GCOO_ERROR_NOT_BUILT: return "GCOO_ERROR_NOT_BUILT";
+    case GCOO_ERROR_UNSUPPORTED: return "GCOO_ERROR_UNSUPPORTED";
+    case GCOO_ERROR_FORMAT: return "GCOO_ERROR_FORMAT";
+    case GCOO_ERROR_TIMEOUT: return "GCOO_ERROR_TIMEOUT";
+    case GCOO_ERROR_CAPACITY: return "GCOO_ERROR_CAPACITY";
+    }
+    return "GCOO_ERROR_UNKNOWN";
+}
+
+const char *gcoo_last_error(void) { return t_last_error.c_str(); }
+
+gcoo_status gcoo_params_default(gcoo_params *p)
+{
+    if (!p)
+        return fail(GCOO_ERROR_INVALID_VALUE, "params is NULL");
+    memset(p, 0, sizeof(*p));
+    p->rows_per_group = 4; // src/constants.h:4 COLUMN_PER_GROUP
+    p->engine = GCOO_ENGINE_AUTO;
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_set_allocator(gcoo_alloc_fn alloc, gcoo_free_fn release, void *ctx)
+{
+    if ((alloc == nullptr) != (release == nullptr))
+        return fail(GCOO_ERROR_INVALID_VALUE, "allocator and free function must be given together");
+    g_alloc = alloc;
+    g_free = release;
+    g_alloc_ctx = ctx;
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_create(gcoo_handle **out, const float *dA, int64_t m, int64_t k, const gcoo_params *params)
+{
+    if (!out)
+        return fail(GCOO_ERROR_INVALID_VALUE, "out is NULL");
+    *out = nullptr;
+    if (!dA)
+        return fail(GCOO_ERROR_INVALID_VALUE, "dense matrix pointer is NULL");
+    gcoo_status s = check_dims(m, k);
+    if (s != GCOO_SUCCESS)
+        return s;
+    gcoo_params p;
+    gcoo_params_default(&p);
+    if (params)
+        p = *params;
+    if (!valid_cpg(p.rows_per_group))
+        return fail(GCOO_ERROR_INVALID_VALUE, "rows_per_group must be a power of two in [1, 32]");
+    if (p.vec != 0 && p.vec != 1 && p.vec != 2 && p.vec != 4)
+        return fail(GCOO_ERROR_INVALID_VALUE, "vec must be 0, 1, 2 or 4");
+    if (p.warps < 0 || p.warps > 32 || p.col_warps < 0 || p.col_warps > 32)
+        return fail(GCOO_ERROR_INVALID_VALUE, "warps / col_warps out of range");
+    if (p.engine < GCOO_ENGINE_AUTO || p.engine > GCOO_ENGINE_TENSOR)
+        return fail(GCOO_ERROR_INVALID_VALUE, "unknown engine");
+    gcoo_handle *h = new (std::nothrow) gcoo_handle();
+    if (!h)
+        return fail(GCOO_ERROR_ALLOC, "host allocation of the handle failed");
+    h->dA = dA;
+    h->m = m;
+    h->k = k;
+    h->p = p;
+    h->ng = (m + p.rows_per_group - 1) / p.rows_per_group;
+    *out = h;
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_build(gcoo_handle *h, void *stream)
+{
+    if (!h)
+        return fail(GCOO_ERROR_INVALID_VALUE, "handle is NULL");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    h->built = false;
+    const size_t sc = scan_scratch_elems(h->m);
+    if (!h->row_ptr.ensure(static_cast<size_t>(h->m) + 1) || !h->groups.ensure(2 * static_cast<size_t>(h->ng + 1)) ||
+        !h->scratch.ensure(sc + 1) || !h->status.ensure(1))
+        return fail(GCOO_ERROR_ALLOC, "device allocation of the GCOO index arrays failed");
+    GCOO_CUDA(cudaMemsetAsync(h->status.ptr, 0, sizeof(uint32_t), st));
+    GCOO_CUDA(launch_row_count(h->dA, h->m, h->k, h->row_ptr.ptr, st));
+    int64_t *d_total = h->scratch.ptr + sc;
+    GCOO_CUDA(launch_row_scan(h->row_ptr.ptr, h->m, h->p.rows_per_group, h->group_index(), h->nnz_per_group(),
+                              d_total, h->scratch.ptr, h->status.ptr, st));
+    int64_t total = 0;
+    GCOO_CUDA(cudaMemcpyAsync(&total, d_total, sizeof(total), cudaMemcpyDeviceToHost, st));
+    GCOO_CUDA(cudaStreamSynchronize(st));
+    if (total < 0 || total > 0x7fffffffLL)
+        return fail(GCOO_ERROR_FORMAT, "nnz = " + std::to_string(total) + " exceeds the int32 GCOO format");
+    const size_t nnz = static_cast<size_t>(total);
+    if (!h->vals.ensure(nnz) || !h->rc.ensure(2 * nnz) || !h->packed.ensure(nnz + 2))
+        return fail(GCOO_ERROR_ALLOC, "device allocation of the GCOO entry arrays failed");
+    // rows and cols live in one block, as in the reference (src/ShGCOOSpDM.cu:95-97)
+    int32_t *rows = h->rc.ptr;
+    int32_t *cols = h->rc.ptr + nnz;
+    GCOO_CUDA(launch_scatter(h->dA, h->m, h->k, h->p.rows_per_group, h->group_index(), h->row_ptr.ptr,
+                             h->vals.ptr, rows, cols, h->packed.ptr, st));
+    h->nnz = total;
+    h->built = true;
+    if (h->tc)
+        destroy_tc_plan(h->tc);
+    h->tc = nullptr;
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_export(const gcoo_handle *h, gcoo_view *out)
+{
+    if (!h || !out)
+        return fail(GCOO_ERROR_INVALID_VALUE, "handle or view is NULL");
+    if (!h->built)
+        return fail(GCOO_ERROR_NOT_BUILT, "gcoo_build has not run");
+    out->m = h->m;
+    out->k = h->k;
+    out->nnz = h->nnz;
+    out->n_group = h->ng;
+    out->rows_per_group = h->p.rows_per_group;
+    out->group_index = h->groups.ptr;
+    out->nnz_per_group = h->groups.ptr + (h->ng + 1);
+    out->vals = h->vals.ptr;
+    out->rows = h->rc.ptr;
+    out->cols = h->rc.ptr + h->nnz;
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, void *stream)
+{
+    if (!h || !dB || !dC)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL handle or matrix pointer");
+    if (!h->built)
+        return fail(GCOO_ERROR_NOT_BUILT, "gcoo_build has not run");
+    gcoo_status s = check_n(n);
+    if (s != GCOO_SUCCESS)
+        return s;
+    return spdm_fp32(h, dB, n, dC, static_cast<cudaStream_t>(stream), nullptr);
+}
+
+gcoo_status gcoo_spdm_ex(gcoo_handle *h, const float *dB, int64_t n, float *dC, gcoo_precision prec, void *stream)
+{
+    if (!h || !dB || !dC)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL handle or matrix pointer");
+    if (!h->built)
+        return fail(GCOO_ERROR_NOT_BUILT, "gcoo_build has not run");
+    gcoo_status s = check_n(n);
+    if (s != GCOO_SUCCESS)
+        return s;
+    if (prec == GCOO_PREC_FP32)
+        return spdm_fp32(h, dB, n, dC, static_cast<cudaStream_t>(stream), nullptr);
+    if (prec < GCOO_PREC_FP32 || prec > GCOO_PREC_FP8_B)
+        return fail(GCOO_ERROR_INVALID_VALUE, "unknown precision");
+    return run_form(h, dB, n, dC, prec, static_cast<cudaStream_t>(stream), false);
+}
+
+gcoo_status gcoo_prepare(gcoo_handle *h, int64_t n, gcoo_precision prec, void *stream)
+{
+    if (!h)
+        return fail(GCOO_ERROR_INVALID_VALUE, "handle is NULL");
+    if (!h->built)
+        return fail(GCOO_ERROR_NOT_BUILT, "gcoo_build has not run");
+    gcoo_status s = check_n(n);
+    if (s != GCOO_SUCCESS)
+        return s;
+    if (prec == GCOO_PREC_FP32)
+        return GCOO_SUCCESS;
+    if (prec < GCOO_PREC_FP32 || prec > GCOO_PREC_FP8_B)
+        return fail(GCOO_ERROR_INVALID_VALUE, "unknown precision");
+    return run_form(h, nullptr, n, nullptr, prec, static_cast<cudaStream_t>(stream), true);
+}
+
+gcoo_status gcoo_multiply_by(gcoo_handle *h, const float *dB, int64_t n, float *dC, void *stream)
+{
+    if (!h || !dB || !dC)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL handle or matrix pointer");
+    gcoo_status s = check_n(n);
+    if (s != GCOO_SUCCESS)
+        return s;
+    s = gcoo_build(h, stream);
+    if (s != GCOO_SUCCESS)
+        return s;
+    return spdm_fp32(h, dB, n, dC, static_cast<cudaStream_t>(stream), nullptr);
+}
+
+gcoo_status gcoo_destroy(gcoo_handle *h)
+{
+    delete h; // DevBuf members release through the allocator
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_query_engine(gcoo_handle *h, gcoo_precision prec, int32_t *tensor)
+{
+    if (!h || !tensor)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL argument");
+    if (!h->built)
+        return fail(GCOO_ERROR_NOT_BUILT, "gcoo_build has not run");
+    *tensor = (prec != GCOO_PREC_FP32 && form_uses_tensor(h, prec)) ? 1 : 0;
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_device_status(gcoo_handle *h, void *stream, uint32_t *status)
+{
+    if (!h || !status)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL argument");
+    *status = 0;
+    if (!h->status.ptr)
+        return GCOO_SUCCESS;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    GCOO_CUDA(cudaMemcpyAsync(status, h->status.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GCOO_CUDA(cudaStreamSynchronize(st));
+    if (*status & kStatusWaitTimeout)
+        return fail(GCOO_ERROR_TIMEOUT, "a bounded device wait gave up");
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_convert_count(const float *dA, int64_t m, int64_t k, int32_t rows_per_group, int32_t *d_group_index,
+                               int32_t *d_nnz_per_group, int64_t *nnz, void *stream)
+{
+    if (!dA || !d_group_index || !d_nnz_per_group || !nnz)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL argument");
+    gcoo_status s = check_dims(m, k);
+    if (s != GCOO_SUCCESS)
+        return s;
+    if (!valid_cpg(rows_per_group))
+        return fail(GCOO_ERROR_INVALID_VALUE, "rows_per_group must be a power of two in [1, 32]");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    DevBuf<int32_t> counts;
+    DevBuf<int64_t> scratch;
+    const size_t sc = scan_scratch_elems(m);
+    if (!counts.ensure(static_cast<size_t>(m) + 1) || !scratch.ensure(sc + 1))
+        return fail(GCOO_ERROR_ALLOC, "device allocation of conversion scratch failed");
+    GCOO_CUDA(launch_row_count(dA, m, k, counts.ptr, st));
+    GCOO_CUDA(launch_row_scan(counts.ptr, m, rows_per_group, d_group_index, d_nnz_per_group, scratch.ptr + sc,
+                              scratch.ptr, nullptr, st));
+    int64_t total = 0;
+    GCOO_CUDA(cudaMemcpyAsync(&total, scratch.ptr + sc, sizeof(total), cudaMemcpyDeviceToHost, st));
+    GCOO_CUDA(cudaStreamSynchronize(st));
+    *nnz = total;
+    if (total > 0x7fffffffLL)
+        return fail(GCOO_ERROR_FORMAT, "nnz exceeds the int32 GCOO format");
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_convert_scatter(const float *dA, int64_t m, int64_t k, int32_t rows_per_group,
+                                 const int32_t *d_group_index, float *d_vals, int32_t *d_rows, int32_t *d_cols,
+                                 void *stream)
+{
+    if (!dA || !d_group_index || !d_vals || !d_rows || !d_cols)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL argument");
+    gcoo_status s = check_dims(m, k);
+    if (s != GCOO_SUCCESS)
+        return s;
+    if (!valid_cpg(rows_per_group))
+        return fail(GCOO_ERROR_INVALID_VALUE, "rows_per_group must be a power of two in [1, 32]");
+    GCOO_CUDA(launch_scatter(dA, m, k, rows_per_group, d_group_index, nullptr, d_vals, d_rows, d_cols, nullptr,
+                             static_cast<cudaStream_t>(stream)));
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_spdm_view(const gcoo_view *a, const float *dB, int64_t n, float *dC, void *stream)
+{
+    if (!a || !dB || !dC || !a->group_index || !a->nnz_per_group)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL argument");
+    if (a->nnz > 0 && (!a->vals || !a->rows || !a->cols))
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL entry arrays");
+    gcoo_status s = check_dims(a->m, a->k);
+    if (s != GCOO_SUCCESS)
+        return s;
+    s = check_n(n);
+    if (s != GCOO_SUCCESS)
+        return s;
+    if (a->rows_per_group < 1 || a->rows_per_group > 32 ||
+        a->n_group != (a->m + a->rows_per_group - 1) / a->rows_per_group)
+        return fail(GCOO_ERROR_INVALID_VALUE, "inconsistent rows_per_group / n_group");
+    GCOO_CUDA(launch_spdm_view(*a, dB, n, dC, static_cast<cudaStream_t>(stream)));
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_error_norm(gcoo_handle *h, const float *dB, int64_t n, const float *dC, double *rel_fro,
+                            void *stream)
+{
+    if (!h || !dB || !dC || !rel_fro)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL argument");
+    if (!h->built)
+        return fail(GCOO_ERROR_NOT_BUILT, "gcoo_build has not run");
+    gcoo_status s = check_n(n);
+    if (s != GCOO_SUCCESS)
+        return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (!h->norm.ensure(2))
+        return fail(GCOO_ERROR_ALLOC, "device allocation failed");
+    GCOO_CUDA(cudaMemsetAsync(h->norm.ptr, 0, 2 * sizeof(double), st));
+    GCOO_CUDA(launch_error_norm(h->packed.ptr, h->row_ptr.ptr, h->m, dB, n, dC, h->norm.ptr, st));
+    double acc[2] = {0.0, 0.0};
+    GCOO_CUDA(cudaMemcpyAsync(acc, h->norm.ptr, sizeof(acc), cudaMemcpyDeviceToHost, st));
+    GCOO_CUDA(cudaStreamSynchronize(st));
+    if (acc[1] == 0.0)
+        *rel_fro = acc[0] == 0.0 ? 0.0 : INFINITY;
+    else
+        *rel_fro = sqrt(acc[0]) / sqrt(acc[1]);
+    return GCOO_SUCCESS;
+}
+
+} // extern "C"

@@ -1,0 +1,41 @@
+// handle.hpp -- the gcoo_handle object behind the C ABI (not installed).
+#pragma once
+
+#include "internal.cuh"
+
+namespace gcoo {
+struct TcPlan;    // tensor-core tiles (spdm_tc.cu)
+struct LowpWork;  // low-precision workspaces (spdm_lowp.cu)
+void destroy_tc_plan(TcPlan *p);
+void destroy_lowp_work(LowpWork *w);
+} // namespace gcoo
+
+struct gcoo_handle {
+    const float *dA = nullptr;
+    int64_t m = 0, k = 0;
+    gcoo_params p{};
+    int64_t ng = 0;
+    bool built = false;
+    int64_t nnz = 0;
+
+    gcoo::DevBuf<int32_t> row_ptr;   // m + 1 (row counts, then exclusive prefix)
+    gcoo::DevBuf<int32_t> groups;    // group_index[ng+1] | nnz_per_group[ng+1]
+    gcoo::DevBuf<float> vals;        // reference GCOO order
+    gcoo::DevBuf<int32_t> rc;        // rows[nnz] | cols[nnz]
+    gcoo::DevBuf<gcoo::Entry> packed; // row order, nnz + 2 (16-byte padded)
+    gcoo::DevBuf<int64_t> scratch;   // scan block sums (+1) and the total
+    gcoo::DevBuf<uint32_t> status;   // device status word
+    gcoo::DevBuf<double> norm;       // error-norm accumulators
+
+    gcoo::TcPlan *tc = nullptr;
+    gcoo::LowpWork *lowp = nullptr;
+
+    int32_t *group_index() { return groups.ptr; }
+    int32_t *nnz_per_group() { return groups.ptr + (ng + 1); }
+
+    ~gcoo_handle()
+    {
+        gcoo::destroy_tc_plan(tc);
+        gcoo::destroy_lowp_work(lowp);
+    }
+};

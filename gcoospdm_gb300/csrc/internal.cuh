@@ -1,0 +1,188 @@
+// internal.cuh -- shared definitions of the GB300 GCOO library (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "gcoo.h"
+
+namespace gcoo {
+
+// ---- status word bits written by kernels -------------------------------------
+enum : uint32_t {
+    kStatusWaitTimeout = 1u << 1, // a bounded mbarrier / flag wait gave up
+    kStatusIndex = 1u << 2,       // an index check failed (entry skipped)
+    kStatusOverflow = 1u << 3     // a count did not fit the int32 format
+};
+
+// Upper bound on polls of one mbarrier wait before a kernel gives up
+// (each try_wait suspends the thread for a hardware-chosen interval).
+constexpr uint32_t kWaitLimit = 1u << 24;
+
+// ---- error reporting -------------------------------------------------------------
+void set_error(const std::string &msg);
+gcoo_status fail(gcoo_status s, const std::string &msg);
+gcoo_status cuda_fail(cudaError_t e, const char *what);
+
+#define GCOO_CUDA(call)                                                     \
+    do {                                                                    \
+        cudaError_t e_ = (call);                                            \
+        if (e_ != cudaSuccess)                                              \
+            return ::gcoo::cuda_fail(e_, #call);                            \
+    } while (0)
+
+#define GCOO_LAUNCH(what)                                                   \
+    do {                                                                    \
+        cudaError_t e_ = cudaGetLastError();                                \
+        if (e_ != cudaSuccess)                                              \
+            return ::gcoo::cuda_fail(e_, what);                             \
+    } while (0)
+
+// Adds n to the process-wide launch counter (gcoo_kernel_launches).
+void count_launches(int n);
+
+// ---- device allocation through the pluggable allocator -----------------------------
+void *dev_alloc(size_t bytes);
+void dev_free(void *p);
+
+template <class T>
+struct DevBuf {
+    T *ptr = nullptr;
+    size_t count = 0; // capacity in elements
+    ~DevBuf() { reset(); }
+    void reset()
+    {
+        if (ptr)
+            dev_free(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+    // Grow (never shrink) to at least n elements; contents are not kept.
+    bool ensure(size_t n)
+    {
+        if (n <= count && ptr)
+            return true;
+        reset();
+        size_t bytes = (n ? n : 1) * sizeof(T);
+        ptr = static_cast<T *>(dev_alloc(bytes));
+        if (!ptr)
+            return false;
+        count = n ? n : 1;
+        return true;
+    }
+};
+
+// One packed entry of the execution layout: column and FP32 value bits.
+struct __align__(8) Entry {
+    int32_t col;
+    float val;
+};
+
+// ---- kernel launchers (convert.cu) ----------------------------------------------------
+// Per-row nonzero counts (row_nnz[0..m)).
+cudaError_t launch_row_count(const float *A, int64_t m, int64_t k, int32_t *row_nnz,
+                             cudaStream_t st);
+// Exclusive scan of row counts into row_ptr[0..m] (in place allowed) and the
+// derived group arrays; *d_total receives the int64 total. scratch needs
+// scan_scratch_elems(m) int64 elements.
+size_t scan_scratch_elems(int64_t m);
+cudaError_t launch_row_scan(int32_t *row_counts_then_ptr, int64_t m, int32_t rows_per_group,
+                            int32_t *group_index, int32_t *nnz_per_group, int64_t *d_total,
+                            int64_t *scratch, uint32_t *status, cudaStream_t st);
+// Group arrays only (count entry point without row pointers): from row counts.
+cudaError_t launch_scatter(const float *A, int64_t m, int64_t k, int32_t rows_per_group,
+                           const int32_t *group_index, const int32_t *row_ptr, float *vals,
+                           int32_t *rows, int32_t *cols, Entry *packed, cudaStream_t st);
+
+// ---- FP32 multiply (spdm_fp32.cu) ------------------------------------------------------
+struct LaunchShape {
+    int vec;       // columns per thread (1, 2, 4)
+    int warps;     // warps per CTA
+    int col_warps; // warps side by side on one row
+};
+LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz,
+                       uintptr_t b_addr, uintptr_t c_addr);
+cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_t m,
+                             int32_t rows_per_group, const float *B, int64_t n, float *C,
+                             const LaunchShape &s, uint32_t *status, cudaStream_t st);
+// Multiply straight from reference-layout GCOO arrays (column-major order
+// inside a group): one thread per column per group row.
+cudaError_t launch_spdm_view(const gcoo_view &a, const float *B, int64_t n, float *C,
+                             cudaStream_t st);
+
+// ---- FP64 check (errnorm.cu) -----------------------------------------------------------
+cudaError_t launch_error_norm(const Entry *packed, const int32_t *row_ptr, int64_t m,
+                              const float *B, int64_t n, const float *C, double *acc2,
+                              cudaStream_t st);
+
+// ---- inline PTX helpers -----------------------------------------------------------------
+#if defined(__CUDACC__)
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Returns true once the phase with the given parity has completed, false if
+// the bounded number of polls ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    const uint32_t addr = smem_u32(bar);
+    for (uint32_t it = 0; it < kWaitLimit; ++it) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done)
+                     : "r"(addr), "r"(parity)
+                     : "memory");
+        if (done)
+            return true;
+    }
+    return false;
+}
+
+// Bulk (non-tensor) async copy global -> shared, completing on `bar`.
+// dst, src 16-byte aligned; bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+                 "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ float4 ldg_f4(const float4 *p) { return __ldg(p); }
+#endif
+
+} // namespace gcoo

@@ -1,0 +1,279 @@
+// spdm_fp32.cu -- the plain FP32 GCOO x dense multiply on sm_103a.
+//
+// Replaces sparse_dense_groupcoo_mat_mul_kernel (src/gcoo_spdm_kernels.cu:
+// 92-158). One CTA per (GCOO group, column tile):
+//   * one elected thread stages the group's nonzeros (the contiguous range
+//     [row_ptr[g*cpg], row_ptr[(g+1)*cpg]) of the packed row-ordered layout)
+//     into shared memory with cp.async.bulk, completing on an mbarrier;
+//   * each warp owns one row of the group and 32*V output columns; for every
+//     entry of its row (a shared-memory broadcast) each lane loads V
+//     consecutive B values with one 128-bit (V=4) coalesced load and updates
+//     V register accumulators with fmaf;
+//   * rows of the group run side by side, so B rows shared by several rows of
+//     a group are served from L1.
+// Every C element is a sequential fmaf chain over its row's entries in
+// column order starting from 0.0f -- the same chain the reference kernel
+// evaluates (its entries of one row are visited in column order too), so
+// the FP32 result is bit-identical to the reference's.
+#include "internal.cuh"
+
+namespace gcoo {
+
+namespace {
+
+constexpr int kChunk = 2048; // entries staged per pass (16 KB)
+constexpr int kSmemBytes = 128 + (kChunk + 2) * static_cast<int>(sizeof(Entry));
+
+template <int V>
+struct Vec;
+template <>
+struct Vec<4> {
+    static __device__ __forceinline__ void load(const float *p, float (&o)[4])
+    {
+        const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+        o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+    }
+    static __device__ __forceinline__ void store(float *p, const float (&o)[4])
+    {
+        *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
+    }
+};
+template <>
+struct Vec<2> {
+    static __device__ __forceinline__ void load(const float *p, float (&o)[2])
+    {
+        const float2 t = __ldg(reinterpret_cast<const float2 *>(p));
+        o[0] = t.x; o[1] = t.y;
+    }
+    static __device__ __forceinline__ void store(float *p, const float (&o)[2])
+    {
+        *reinterpret_cast<float2 *>(p) = make_float2(o[0], o[1]);
+    }
+};
+template <>
+struct Vec<1> {
+    static __device__ __forceinline__ void load(const float *p, float (&o)[1]) { o[0] = __ldg(p); }
+    static __device__ __forceinline__ void store(float *p, const float (&o)[1]) { *p = o[0]; }
+};
+
+template <int V, int U>
+__device__ __forceinline__ void row_chain(const Entry *__restrict__ s, int cnt, const float *__restrict__ Bj,
+                                          int64_t n, float (&acc)[V])
+{
+    int i = 0;
+#pragma unroll 1
+    for (; i + U <= cnt; i += U) {
+        Entry e[U];
+        float b[U][V];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            e[u] = s[i + u];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            Vec<V>::load(Bj + static_cast<int64_t>(e[u].col) * n, b[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                acc[v] = fmaf(e[u].val, b[u][v], acc[v]);
+    }
+#pragma unroll 1
+    for (; i < cnt; ++i) {
+        const Entry e = s[i];
+        float b[V];
+        Vec<V>::load(Bj + static_cast<int64_t>(e.col) * n, b);
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+            acc[v] = fmaf(e.val, b[v], acc[v]);
+    }
+}
+
+// MAXT bounds the CTA size (rows_per_group * col_warps warps); the 1024-thread
+// variant (rows_per_group 32) unrolls less to stay within 64 registers.
+template <int V, int MAXT>
+__global__ void __launch_bounds__(MAXT)
+spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ row_ptr, int64_t m,
+                 int32_t cpg, const float *__restrict__ B, int64_t n, float *__restrict__ C,
+                 int32_t col_warps, uint32_t *__restrict__ status)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    Entry *s_nz = reinterpret_cast<Entry *>(smem + 128);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int slot = warp / col_warps, sub = warp - slot * col_warps;
+    const int64_t r0 = static_cast<int64_t>(blockIdx.x) * cpg;
+    const int64_t r_end = r0 + cpg < m ? r0 + cpg : m;
+    const int64_t row = r0 + slot;
+    const bool has_row = slot < cpg && row < r_end;
+    const int64_t j = (static_cast<int64_t>(blockIdx.y) * col_warps + sub) * (32 * V) + static_cast<int64_t>(lane) * V;
+    const bool has_col = j < n;
+
+    const int64_t gs = row_ptr[r0];
+    const int64_t ge = row_ptr[r_end];
+    int64_t rs = 0, re = 0;
+    if (has_row) {
+        rs = row_ptr[row];
+        re = row_ptr[row + 1];
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    float acc[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+        acc[v] = 0.0f;
+    const float *Bj = B + j;
+
+    const int64_t total = ge - gs;
+    const int64_t nchunks = (total + kChunk - 1) / kChunk;
+    bool ok = true;
+    for (int64_t ch = 0; ch < nchunks && ok; ++ch) {
+        const int64_t cs = gs + ch * kChunk;
+        const int64_t ce = cs + kChunk < ge ? cs + kChunk : ge;
+        const int64_t a0 = cs & ~static_cast<int64_t>(1); // 16-byte aligned superset
+        const int64_t a1 = (ce + 1) & ~static_cast<int64_t>(1);
+        if (threadIdx.x == 0) {
+            fence_proxy_async();
+            const uint32_t bytes = static_cast<uint32_t>((a1 - a0) * static_cast<int64_t>(sizeof(Entry)));
+            mbar_arrive_expect_tx(bar, bytes);
+            bulk_g2s(s_nz, packed + a0, bytes, bar);
+        }
+        const bool waited = mbar_wait(bar, static_cast<uint32_t>(ch & 1));
+        ok = __syncthreads_and(waited) != 0;
+        if (!ok) {
+            if (threadIdx.x == 0)
+                atomicOr(status, kStatusWaitTimeout);
+            mbar_wait(bar, static_cast<uint32_t>(ch & 1)); // let the copy in flight land
+            break;
+        }
+        const int64_t lo = rs > cs ? rs : cs;
+        const int64_t hi = re < ce ? re : ce;
+        if (has_col && lo < hi)
+            row_chain<V, (MAXT > 512 ? 4 : 8)>(s_nz + (lo - a0), static_cast<int>(hi - lo), Bj, n, acc);
+        __syncthreads(); // buffer free before the next copy
+    }
+    if (has_row && has_col && ok)
+        Vec<V>::store(C + row * n + j, acc);
+}
+
+// Multiply straight from reference-layout arrays (entries of a group in
+// column-then-row order, separate vals/rows/cols): one thread per output
+// column, one shared-memory accumulator per (group row, column) so any
+// rows_per_group works; each accumulator still sees its row's entries in
+// column order, hence the same fmaf chain.
+constexpr int kViewThreads = 128;
+__global__ void __launch_bounds__(kViewThreads)
+spdm_view_kernel(const float *__restrict__ vals, const int32_t *__restrict__ rows,
+                 const int32_t *__restrict__ cols, const int32_t *__restrict__ group_index,
+                 const int32_t *__restrict__ nnz_per_group, int64_t m, int32_t cpg,
+                 const float *__restrict__ B, int64_t n, float *__restrict__ C)
+{
+    extern __shared__ float s_acc[]; // [cpg][kViewThreads]
+    const int64_t g = blockIdx.x;
+    const int64_t r0 = g * cpg;
+    const int64_t j = static_cast<int64_t>(blockIdx.y) * kViewThreads + threadIdx.x;
+    for (int r = 0; r < cpg; ++r)
+        s_acc[r * kViewThreads + threadIdx.x] = 0.0f;
+    const int64_t e0 = group_index[g];
+    const int64_t e1 = e0 + nnz_per_group[g];
+    if (j < n) {
+        for (int64_t e = e0; e < e1; ++e) {
+            const int32_t lr = rows[e] - static_cast<int32_t>(r0);
+            if (lr < 0 || lr >= cpg)
+                continue; // not this group's row: malformed input, skipped
+            float *a = s_acc + lr * kViewThreads + threadIdx.x;
+            *a = fmaf(vals[e], __ldg(B + static_cast<int64_t>(cols[e]) * n + j), *a);
+        }
+        for (int r = 0; r < cpg && r0 + r < m; ++r)
+            C[(r0 + r) * n + j] = s_acc[r * kViewThreads + threadIdx.x];
+    }
+}
+
+} // namespace
+
+LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, uintptr_t b_addr,
+                       uintptr_t c_addr)
+{
+    (void)m;
+    (void)nnz;
+    LaunchShape s;
+    int vmax = 4;
+    if (n % 4 != 0 || (b_addr & 15) || (c_addr & 15))
+        vmax = 2;
+    if (vmax == 2 && (n % 2 != 0 || (b_addr & 7) || (c_addr & 7)))
+        vmax = 1;
+    int v = p.vec > 0 ? p.vec : (n >= 128 ? 4 : (n >= 64 ? 2 : 1));
+    if (v > vmax)
+        v = vmax;
+    if (v != 1 && v != 2 && v != 4)
+        v = 1;
+    s.vec = v;
+    const int cpg = p.rows_per_group;
+    int cw;
+    if (p.col_warps > 0)
+        cw = p.col_warps;
+    else {
+        const int target = p.warps > 0 ? p.warps : 8;
+        cw = target / cpg;
+        if (cw < 1)
+            cw = 1;
+        // no wider than the matrix
+        while (cw > 1 && static_cast<int64_t>(cw / 2) * 32 * v >= n)
+            cw /= 2;
+    }
+    if (cw * cpg > 32)
+        cw = 32 / cpg > 0 ? 32 / cpg : 1;
+    s.col_warps = cw;
+    s.warps = cw * cpg;
+    return s;
+}
+
+cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_t m, int32_t cpg,
+                             const float *B, int64_t n, float *C, const LaunchShape &s, uint32_t *status,
+                             cudaStream_t st)
+{
+    const int64_t ng = (m + cpg - 1) / cpg;
+    const int64_t tile = static_cast<int64_t>(s.col_warps) * 32 * s.vec;
+    const int64_t ny = (n + tile - 1) / tile;
+    if (ng <= 0 || ny <= 0)
+        return cudaSuccess;
+    if (ny > 65535)
+        return cudaErrorInvalidConfiguration;
+    dim3 grid(static_cast<unsigned>(ng), static_cast<unsigned>(ny));
+    const int threads = s.warps * 32;
+#define GCOO_FP32_LAUNCH(V, T)                                                                          \
+    spdm_fp32_kernel<V, T><<<grid, threads, kSmemBytes, st>>>(packed, row_ptr, m, cpg, B, n, C, s.col_warps, status)
+    if (threads <= 512) {
+        if (s.vec == 4) GCOO_FP32_LAUNCH(4, 512);
+        else if (s.vec == 2) GCOO_FP32_LAUNCH(2, 512);
+        else GCOO_FP32_LAUNCH(1, 512);
+    } else {
+        if (s.vec == 4) GCOO_FP32_LAUNCH(4, 1024);
+        else if (s.vec == 2) GCOO_FP32_LAUNCH(2, 1024);
+        else GCOO_FP32_LAUNCH(1, 1024);
+    }
+#undef GCOO_FP32_LAUNCH
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spdm_view(const gcoo_view &a, const float *B, int64_t n, float *C, cudaStream_t st)
+{
+    if (a.n_group <= 0 || n <= 0)
+        return cudaSuccess;
+    const int64_t ny = (n + kViewThreads - 1) / kViewThreads;
+    if (ny > 65535)
+        return cudaErrorInvalidConfiguration;
+    dim3 grid(static_cast<unsigned>(a.n_group), static_cast<unsigned>(ny));
+    const size_t smem = sizeof(float) * static_cast<size_t>(a.rows_per_group) * kViewThreads;
+    spdm_view_kernel<<<grid, kViewThreads, smem, st>>>(a.vals, a.rows, a.cols, a.group_index, a.nnz_per_group,
+                                                       a.m, a.rows_per_group, B, n, C);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+} // namespace gcoo

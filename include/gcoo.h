@@ -1,0 +1,233 @@
+/*
+ * gcoo.h -- C ABI of the GB300 (sm_103a) GCOO sparse x dense multiply.
+ *
+ * Drop-in boundary for the reference's -algo=gcoospdm path (hclhkbu/gcoospdm):
+ * the C++ plugin classes in ShGemm.h / ShGCOOSpDM.h / SpGemmBuilder.h are thin
+ * shims over these entry points, and any FFI (ctypes, cgo, JNI) can bind them
+ * directly. Plain pointers and sizes only; every device pointer is a CUDA
+ * device address on the current device; `stream` is a cudaStream_t (NULL =
+ * legacy default stream).
+ *
+ * Orientation (row-major, as the reference kernel indexes its operands):
+ *   A  m x k sparse operand, given as a dense FP32 buffer holding zeros
+ *      (the reference ctor's `denseMatrix`, src/ShGCOOSpDM.cu:13-17)
+ *   B  k x n dense FP32 (the `A` argument of mutiplyBy, src/ShGCOOSpDM.cu:131)
+ *   C  m x n FP32, C[r*n+j] = sum_c A[r*k+c] * B[c*n+j]
+ *
+ * GCOO format (src/ShGCOOSpDM.h:25-32, src/gcoo_spdm_kernels.cu:30-90): rows
+ * are grouped `rows_per_group` at a time (the reference's COLUMN_PER_GROUP,
+ * 4); nGroup = ceil(m / rows_per_group); group_index[nGroup+1] is the
+ * exclusive prefix of nnz_per_group[nGroup+1] (whose last entry is 0); inside
+ * a group the entries are ordered by column, then row; rows are absolute.
+ * A value is an entry iff `v != 0` (-0.0 is dropped, NaN is kept).
+ *
+ * Errors: every call returns a gcoo_status; nothing exits or throws.
+ * gcoo_last_error() gives a message for the last failure on this thread.
+ * Threading: a handle is not thread-safe; distinct handles may be used
+ * concurrently from different threads and streams.
+ */
+#ifndef GCOO_H
+#define GCOO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GCOO_ABI_VERSION 1
+
+typedef enum gcoo_status {
+    GCOO_SUCCESS = 0,
+    GCOO_ERROR_INVALID_VALUE = 1, /* null pointer, bad size, overflow     */
+    GCOO_ERROR_ALLOC = 2,         /* device allocation failed             */
+    GCOO_ERROR_CUDA = 3,          /* a CUDA call or kernel launch failed  */
+    GCOO_ERROR_NOT_BUILT = 4,     /* multiply before gcoo_build           */
+    GCOO_ERROR_UNSUPPORTED = 5,   /* request this build cannot serve      */
+    GCOO_ERROR_FORMAT = 6,        /* nnz does not fit the int32 format    */
+    GCOO_ERROR_TIMEOUT = 7,       /* a bounded device wait gave up        */
+    GCOO_ERROR_CAPACITY = 8       /* caller-provided buffer too small     */
+} gcoo_status;
+
+/* Arithmetic forms of the multiply. All accumulate in FP32 and write FP32 C. */
+typedef enum gcoo_precision {
+    GCOO_PREC_FP32 = 0,       /* plain form; bit-identical to the reference  */
+    GCOO_PREC_BF16 = 1,       /* A values and B rounded to BF16              */
+    GCOO_PREC_SPLIT_BF16 = 2, /* hi+lo BF16 split, three products            */
+    GCOO_PREC_FP8_B = 3       /* B as FP8 E4M3 with per-column scales        */
+} gcoo_precision;
+
+/* Which execution engine a non-FP32 form may use. */
+typedef enum gcoo_engine {
+    GCOO_ENGINE_AUTO = 0,      /* tensor cores where 16-wide blocks densify */
+    GCOO_ENGINE_CUDA_CORE = 1, /* FMA pipes only                             */
+    GCOO_ENGINE_TENSOR = 2     /* tcgen05 tensor cores                       */
+} gcoo_engine;
+
+/* Runtime replacement of the reference's compile-time tile constants
+ * (src/constants.h:4-5, filled by src/autotune.py from constants.h.t). */
+typedef struct gcoo_params {
+    int32_t rows_per_group; /* GCOO group height (reference: 4), 1..32     */
+    int32_t vec;            /* output columns per thread: 0 auto, 1, 2, 4   */
+    int32_t warps;          /* warps per CTA: 0 auto, 1..32                 */
+    int32_t col_warps;      /* warps side by side on one row: 0 auto        */
+    int32_t engine;         /* gcoo_engine for non-FP32 forms               */
+    int32_t reserved[3];
+} gcoo_params;
+
+typedef struct gcoo_handle gcoo_handle;
+
+/* Device views of a handle's GCOO arrays (owned by the handle). */
+typedef struct gcoo_view {
+    int64_t m, k, nnz, n_group;
+    int32_t rows_per_group;
+    const int32_t *group_index;   /* [n_group + 1]                         */
+    const int32_t *nnz_per_group; /* [n_group + 1], last entry 0           */
+    const float *vals;            /* [nnz]                                 */
+    const int32_t *rows;          /* [nnz]                                 */
+    const int32_t *cols;          /* [nnz]                                 */
+} gcoo_view;
+
+/* ---- status, version ---------------------------------------------------- */
+int gcoo_abi_version(void);
+const char *gcoo_status_string(gcoo_status s);
+const char *gcoo_last_error(void);
+
+/* Defaults: rows_per_group 4 (the reference's COLUMN_PER_GROUP), the rest
+ * chosen per shape at launch. */
+gcoo_status gcoo_params_default(gcoo_params *p);
+
+/* Device allocator used for every buffer a handle owns (NULL, NULL restores
+ * cudaMalloc/cudaFree). Lets a host framework pool memory, and lets tests
+ * inject allocation failures. Not thread-safe; set it before creating
+ * handles. */
+typedef void *(*gcoo_alloc_fn)(size_t bytes, void *ctx);
+typedef void (*gcoo_free_fn)(void *ptr, void *ctx);
+gcoo_status gcoo_set_allocator(gcoo_alloc_fn alloc, gcoo_free_fn release, void *ctx);
+
+/* ---- the plugin path ----------------------------------------------------- */
+
+/* ShGCOOSpDM(denseMatrix, nRows, nCols) (src/ShGCOOSpDM.cu:13-17): records
+ * the dense sparse operand; nothing runs on the GPU. The handle does not own
+ * dA, which must stay valid while the handle builds from it. */
+gcoo_status gcoo_create(gcoo_handle **out, const float *dA, int64_t m, int64_t k,
+                        const gcoo_params *params);
+
+/* build() (src/ShGCOOSpDM.cu:182-193): dense -> GCOO conversion into
+ * handle-owned arrays (count, device exclusive scan, stable scatter). Reads
+ * the total nnz back to size the arrays, so it synchronises `stream` once.
+ * Calling it again re-converts (dA may have changed). */
+gcoo_status gcoo_build(gcoo_handle *h, void *stream);
+
+gcoo_status gcoo_export(const gcoo_handle *h, gcoo_view *out);
+
+/* runKernelTest() (src/ShGCOOSpDM.cu:195-213): C = A * B with the GCOO
+ * built by gcoo_build, FP32 form. No allocation, no synchronisation; safe
+ * to capture in a CUDA graph. dB is k x n, dC is m x n, row-major. */
+gcoo_status gcoo_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, void *stream);
+
+/* The same multiply in another arithmetic form. The first call for a form
+ * (or a larger n) sizes that form's workspace and, for the tensor-core
+ * engine, builds the densified block tiles: allocation and one
+ * synchronisation happen then, never on later calls of the same shape. */
+gcoo_status gcoo_spdm_ex(gcoo_handle *h, const float *dB, int64_t n, float *dC,
+                         gcoo_precision prec, void *stream);
+
+/* Prepares a form's workspace and tiles for width n without multiplying, so
+ * that later gcoo_spdm_ex calls can be captured in a CUDA graph. */
+gcoo_status gcoo_prepare(gcoo_handle *h, int64_t n, gcoo_precision prec, void *stream);
+
+/* mutiplyBy() (src/ShGCOOSpDM.cu:131-180): conversion + multiply in one call
+ * (FP32). Reuses the handle's arrays when they are large enough, so a steady
+ * loop allocates nothing; it synchronises once to read the nnz, as the
+ * reference does. */
+gcoo_status gcoo_multiply_by(gcoo_handle *h, const float *dB, int64_t n, float *dC, void *stream);
+
+gcoo_status gcoo_destroy(gcoo_handle *h);
+
+/* Form the handle would use for `prec` at width n: writes 1 to *tensor when
+ * the tcgen05 block path is taken. Builds nothing. */
+gcoo_status gcoo_query_engine(gcoo_handle *h, gcoo_precision prec, int32_t *tensor);
+
+/* Number of kernels this library has launched in this process (all
+ * handles, all entry points); lets a caller count launches in a region. */
+uint64_t gcoo_kernel_launches(void);
+
+/* Device status word of the handle's kernels (0 = fine; bit 1: a bounded
+ * wait gave up; bit 2: an index check failed). Synchronises `stream`. */
+gcoo_status gcoo_device_status(gcoo_handle *h, void *stream, uint32_t *status);
+
+/* ---- conversion and multiply on caller-owned arrays ------------------------ */
+
+/* Count + exclusive scan of convertToGroupCOOFormat (src/ShGCOOSpDM.cu:
+ * 33-84): fills group_index and nnz_per_group ([n_group+1] each) and returns
+ * the total in *nnz (synchronises `stream`). */
+gcoo_status gcoo_convert_count(const float *dA, int64_t m, int64_t k, int32_t rows_per_group,
+                               int32_t *d_group_index, int32_t *d_nnz_per_group, int64_t *nnz,
+                               void *stream);
+
+/* Stable scatter of convertToGroupCOOFormat (src/ShGCOOSpDM.cu:94-111,
+ * src/gcoo_spdm_kernels.cu:30-90) into caller arrays of at least nnz
+ * entries, using a group_index produced by gcoo_convert_count. */
+gcoo_status gcoo_convert_scatter(const float *dA, int64_t m, int64_t k, int32_t rows_per_group,
+                                 const int32_t *d_group_index, float *d_vals, int32_t *d_rows,
+                                 int32_t *d_cols, void *stream);
+
+/* sparse_dense_groupcoo_mat_mul_kernel (src/gcoo_spdm_kernels.cu:92-158) on
+ * caller-owned GCOO arrays in the reference layout, FP32, any
+ * rows_per_group; result bit-identical to gcoo_spdm. */
+gcoo_status gcoo_spdm_view(const gcoo_view *a, const float *dB, int64_t n, float *dC, void *stream);
+
+/* ---- checks ---------------------------------------------------------------- */
+
+/* Relative Frobenius error ||C - A*B||_F / ||A*B||_F with A*B accumulated in
+ * FP64 on the GPU (the only FP64 work in the library). Synchronises. */
+gcoo_status gcoo_error_norm(gcoo_handle *h, const float *dB, int64_t n, const float *dC,
+                            double *rel_fro, void *stream);
+
+/* ---- batched, persistent ---------------------------------------------------- */
+
+typedef struct gcoo_problem {
+    gcoo_handle *a; /* built handle */
+    const float *dB;
+    int64_t n;
+    float *dC;
+} gcoo_problem;
+
+typedef struct gcoo_batch gcoo_batch;
+
+/* Plans many independent multiplies for one persistent launch: work items
+ * (problem, group range, column tile) sorted by nnz, descending, in a device
+ * queue; tile parameters per shape bucket from the autotune table when one is
+ * loaded. prec: GCOO_PREC_FP32 or GCOO_PREC_BF16. Allocates; synchronises. */
+gcoo_status gcoo_batch_create(gcoo_batch **out, const gcoo_problem *problems, int32_t count,
+                              gcoo_precision prec, void *stream);
+
+/* One persistent launch over the whole queue (replayed from a CUDA graph
+ * after the first call). No allocation. */
+gcoo_status gcoo_batch_run(gcoo_batch *b, void *stream);
+
+/* Number of kernel launches one gcoo_batch_run performs. */
+gcoo_status gcoo_batch_launches(const gcoo_batch *b, int32_t *launches);
+
+gcoo_status gcoo_batch_destroy(gcoo_batch *b);
+
+/* ---- autotuner ---------------------------------------------------------------- */
+
+/* Times the candidate (vec, warps, col_warps) settings for this handle at
+ * width n (FP32 form) on `stream` and stores the fastest in the in-process
+ * table under the shape bucket of (m, k, nnz, n). Writes the winner to
+ * *best when not NULL. Synchronises. */
+gcoo_status gcoo_autotune(gcoo_handle *h, const float *dB, int64_t n, float *dC, void *stream,
+                          gcoo_params *best);
+
+/* Persist / load the table as JSON (one object per bucket). */
+gcoo_status gcoo_autotune_save(const char *path);
+gcoo_status gcoo_autotune_load(const char *path);
+gcoo_status gcoo_autotune_clear(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,189 @@
+"""GPU: the plain FP32 multiply through the C ABI, bit-identical to the
+reference's output (golden fixtures) and to the oracle; relative Frobenius
+error against FP64 at the full benchmark size."""
+from __future__ import annotations
+
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_inputs
+
+pytestmark = pytest.mark.gpu
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def dev(torch, x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def same_bits(x, y):
+    """Bitwise equality, NaNs compared as NaN (payloads differ across ISAs)."""
+    x, y = np.asarray(x, np.float32), np.asarray(y, np.float32)
+    nx, ny = np.isnan(x), np.isnan(y)
+    return bool(np.array_equal(nx, ny) and np.array_equal(x[~nx].view(np.uint32), y[~ny].view(np.uint32)))
+
+
+WITH_C = ["tiny", "edge_values", "empty_groups", "all_zero", "k1", "m3", "n_tail", "readme_800",
+          "sweep_2048_s099", "ragged_1001x517"]
+
+
+@pytest.mark.parametrize("name", WITH_C)
+def test_spdm_matches_reference_output(native, oracle_mod, torch, manifest, name):
+    entry = manifest["cases"][name]
+    A, B = golden_inputs(entry, name)
+    h = native.GcooHandle(dev(torch, A)).build()
+    Cg = h.spdm(dev(torch, B)).cpu().numpy()
+    if name == "edge_values":
+        ref = oracle_mod.spdm(oracle_mod.convert(A), B)  # oracle == reference bit-for-bit on this case
+        assert digest(ref) == entry["digests"]["C"]
+        assert same_bits(Cg, ref)
+    else:
+        assert digest(Cg) == entry["digests"]["C"]
+    assert h.device_status() == 0
+
+
+@pytest.mark.parametrize("vec,warps,col_warps", [(1, 0, 0), (2, 0, 0), (4, 0, 0), (4, 4, 1), (4, 16, 4),
+                                                 (2, 8, 2), (1, 32, 8)])
+def test_launch_shapes_bit_identical(native, oracle_mod, torch, vec, warps, col_warps):
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense(21, 1000, 900, 0.03)
+    B = dg.dense_pm1(21, 5, 900, 520)
+    ref = oracle_mod.spdm(oracle_mod.convert(A), B)
+    h = native.GcooHandle(dev(torch, A), vec=vec, warps=warps, col_warps=col_warps).build()
+    assert same_bits(h.spdm(dev(torch, B)).cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("cpg", [1, 2, 8, 16, 32])
+def test_any_group_height_same_result(native, oracle_mod, torch, cpg):
+    """The per-element fmaf chain does not depend on the group height."""
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense(22, 777, 640, 0.02)
+    B = dg.dense_pm1(22, 5, 640, 256)
+    ref = oracle_mod.spdm(oracle_mod.convert(A, 4), B)
+    h = native.GcooHandle(dev(torch, A), rows_per_group=cpg).build()
+    assert same_bits(h.spdm(dev(torch, B)).cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("n", [1, 3, 31, 33, 130, 257, 1000])
+def test_odd_widths(native, oracle_mod, torch, n):
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense(23, 150, 120, 0.1)
+    B = dg.dense_pm1(23, 5, 120, n)
+    ref = oracle_mod.spdm(oracle_mod.convert(A), B)
+    h = native.GcooHandle(dev(torch, A)).build()
+    assert same_bits(h.spdm(dev(torch, B)).cpu().numpy(), ref)
+
+
+def test_misaligned_operands(native, oracle_mod, torch):
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense(24, 200, 160, 0.05)
+    B = dg.dense_pm1(24, 5, 160, 128)
+    ref = oracle_mod.spdm(oracle_mod.convert(A), B)
+    h = native.GcooHandle(dev(torch, A)).build()
+    bufB = torch.zeros(B.size + 1, device="cuda")
+    bufB[1:] = dev(torch, B.ravel())
+    bufC = torch.zeros(200 * 128 + 1, device="cuda")
+    Bv, Cv = bufB[1:].view(160, 128), bufC[1:].view(200, 128)
+    h.spdm(Bv, Cv)
+    assert same_bits(Cv.cpu().numpy(), ref)
+
+
+def test_heavy_group_multi_chunk(native, oracle_mod, torch):
+    """A group with more entries than one shared-memory chunk (2048)."""
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense(25, 40, 6000, 0.002)
+    A[1, :] = dg.dense_pm1(25, 9, 1, 6000)[0]
+    A[2, ::2] = dg.dense_pm1(25, 10, 1, 3000)[0]
+    B = dg.dense_pm1(25, 5, 6000, 200)
+    ref = oracle_mod.spdm(oracle_mod.convert(A), B)
+    h = native.GcooHandle(dev(torch, A)).build()
+    assert same_bits(h.spdm(dev(torch, B)).cpu().numpy(), ref)
+
+
+def test_reference_layout_view_entry(native, oracle_mod, torch, manifest):
+    """gcoo_spdm_view on arrays in the reference's own layout."""
+    for name in ("readme_800", "n_tail", "empty_groups"):
+        entry = manifest["cases"][name]
+        A, B = golden_inputs(entry, name)
+        g = oracle_mod.convert(A)
+        Cg = native.spdm_view(g.m, g.k, 4, dev(torch, g.groupIndex), dev(torch, g.nnzPerGroup),
+                              dev(torch, g.vals), dev(torch, g.rows), dev(torch, g.cols), dev(torch, B))
+        assert digest(Cg.cpu().numpy()) == entry["digests"]["C"], name
+
+
+def test_plugin_mirror_and_builder(native, torch, manifest):
+    entry = manifest["cases"]["readme_800"]
+    A, B = golden_inputs(entry, "readme_800")
+    dA, dB = dev(torch, A), dev(torch, B)
+    C1 = torch.empty(800, 800, device="cuda")
+    g = native.SpGemmBuilder.getShGemmAlgo(dA, 800, 800, "gcoospdm")
+    assert g.mutiplyBy(dB, 800, 800, C1) == 0.0
+    assert digest(C1.cpu().numpy()) == entry["digests"]["C"]
+    g.build()
+    assert g.m_nGroup == 200 and int(g.m_pGroupIndex[-1]) == entry["nnz"]
+    C2 = torch.empty_like(C1)
+    assert g.runKernelTest(dB, 800, 800, C2) == 0.0
+    assert torch.equal(C1, C2)
+    assert native.SpGemmBuilder.getShGemmAlgo(dA, 800, 800, "csr") is None
+    with pytest.raises(native.GcooError):
+        g.mutiply(dB, 800, 800, C2)
+
+
+def test_multiply_by_steady_state_and_determinism(native, torch):
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense(26, 2048, 2048, 0.01)
+    B = dg.dense_pm1(26, 5, 2048, 2048)
+    h = native.GcooHandle(dev(torch, A))
+    dB = dev(torch, B)
+    C1 = h.multiply_by(dB)
+    C2 = h.multiply_by(dB)
+    C3 = h.spdm(dB)
+    assert torch.equal(C1, C2) and torch.equal(C1, C3)
+
+
+def test_error_norm_kernel_matches_oracle(native, oracle_mod, torch):
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense(27, 500, 400, 0.05)
+    B = dg.dense_pm1(27, 5, 400, 300)
+    h = native.GcooHandle(dev(torch, A)).build()
+    Cg = h.spdm(dev(torch, B))
+    e_gpu = h.error_norm(dev(torch, B), Cg)
+    C64 = oracle_mod.dense_gemm_f64(A, B)
+    e_cpu = oracle_mod.rel_fro(Cg.cpu().numpy(), C64)
+    assert e_gpu == pytest.approx(e_cpu, rel=1e-6, abs=1e-12)
+    assert e_gpu < 1e-6
+    # a planted error is seen
+    Cbad = Cg.clone()
+    Cbad[3, 7] += 1.0
+    assert h.error_norm(dev(torch, B), Cbad) > 1e-4
+
+
+def test_full_size_fp32_within_tolerance(native, torch):
+    """n=8192, s=0.99 (the headline point): ||C - C64||_F / ||C64||_F <= 1e-5."""
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense(8192, 8192, 8192, 0.01)
+    B = dg.dense_pm1(8192, 5, 8192, 8192)
+    h = native.GcooHandle(dev(torch, A)).build()
+    dB = dev(torch, B)
+    Cg = h.spdm(dB)
+    err = h.error_norm(dB, Cg)
+    assert err <= 1e-5
+    # and equal, bit for bit, to the oracle on a slice of rows
+    rows = slice(4096, 4096 + 64)
+    sub = A[rows]
+    from oracle import convert, spdm
+    ref = spdm(convert(sub), B)
+    assert np.array_equal(Cg[rows].cpu().numpy().view(np.uint32), ref.view(np.uint32))
