@@ -51,7 +51,7 @@ class _DevArray:
     """__cuda_array_interface__ wrapper: a torch view of library-owned memory."""
 
     def __init__(self, ptr, n, typestr):
-        self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": typestr, "data": (int(ptr or 0), True),
+        self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": typestr, "data": (int(ptr or 0), False),
                                          "version": 3, "strides": None}
 
 

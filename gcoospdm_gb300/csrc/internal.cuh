@@ -17,9 +17,11 @@ enum : uint32_t {
     kStatusOverflow = 1u << 3     // a count did not fit the int32 format
 };
 
-// Upper bound on polls of one mbarrier wait before a kernel gives up
-// (each try_wait suspends the thread for a hardware-chosen interval).
-constexpr uint32_t kWaitLimit = 1u << 24;
+// Bounds of one mbarrier wait before a kernel gives up and reports
+// kStatusWaitTimeout: a wall-clock limit read from %globaltimer, and a poll
+// count (each try_wait suspends the thread for a hardware-chosen interval).
+constexpr uint64_t kWaitNs = 2000000000ull; // 2 s: no legitimate copy or MMA takes this long
+constexpr uint32_t kWaitLimit = 1u << 26;
 
 // ---- error reporting -------------------------------------------------------------
 void set_error(const std::string &msg);
@@ -152,11 +154,19 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Returns true once the phase with the given parity has completed, false if
-// the bounded number of polls ran out.
+// it has not completed within kWaitNs nanoseconds (or kWaitLimit polls).
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
 {
     const uint32_t addr = smem_u32(bar);
+    uint64_t t0 = 0;
     for (uint32_t it = 0; it < kWaitLimit; ++it) {
         uint32_t done;
         asm volatile("{\n\t.reg .pred p;\n\t"
@@ -167,6 +177,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
                      : "memory");
         if (done)
             return true;
+        const uint64_t now = global_ns();
+        if (it == 0)
+            t0 = now;
+        else if (now - t0 > kWaitNs)
+            return false;
     }
     return false;
 }

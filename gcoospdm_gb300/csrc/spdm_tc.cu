@@ -1,0 +1,433 @@
+// spdm_tc.cu -- tensor-core (tcgen05) engine for matrices whose nonzeros
+// densify into 16-wide blocks.
+//
+// Plan (built once per handle and form, from the GCOO entries):
+//   * A is cut into panels of 128 rows; a tile is the 128 x 16 slice of a
+//     panel at column block cb; a tile is active when it holds any entry;
+//   * each active tile is stored densely (zeros where A has none) as BF16 in
+//     the K-major, 32-byte-swizzled shared-memory layout of tcgen05 (row r at
+//     r*32 bytes, 16-byte chunk c at (c ^ ((r >> 2) & 1)) * 16), so one 4 KB
+//     bulk copy lands it ready for the MMA; split-BF16 keeps a second (lo)
+//     tile;
+//   * B is converted per call into tiles of N output columns x 16 k (the
+//     same layout, N rows of 32 bytes).
+// Kernel: one CTA per (panel, N-column tile); warp 0 streams the panel's
+// active tiles through an S-stage ring of shared-memory slots with
+// cp.async.bulk on mbarriers, warp 1 issues one tcgen05.mma kind::f16
+// (M=128, N, K=16; three for split-BF16) per tile into an FP32 accumulator in
+// tensor memory, tcgen05.commit frees each slot, and all four warps drain the
+// accumulator with tcgen05.ld into C. Every wait is bounded.
+#include <cuda_bf16.h>
+
+#include "handle.hpp"
+
+namespace gcoo {
+
+constexpr int kPanel = 128;   // rows per tile (MMA M)
+constexpr int kTileK = 16;    // columns per tile (MMA K)
+constexpr int kTileBytes = kPanel * kTileK * 2;
+
+struct TcPlan {
+    int64_t panels = 0, kb = 0, tiles = 0;
+    bool split = false;
+    int64_t nnz = 0;
+    DevBuf<int32_t> pf;       // exclusive prefix over (panel, cb) flags, size panels*kb + 1
+    DevBuf<int32_t> tile_cb;  // cb of each tile (ascending within a panel)
+    DevBuf<uint16_t> a_hi;    // tiles * 2048 bf16 (swizzled)
+    DevBuf<uint16_t> a_lo;    // split only
+    DevBuf<int64_t> scratch;
+    // B workspace (per call)
+    DevBuf<uint16_t> b_hi, b_lo;
+    int64_t b_n = 0;
+};
+
+void destroy_tc_plan(TcPlan *p) { delete p; }
+
+namespace {
+
+// ---- small PTX wrappers for tcgen05 ----------------------------------------------
+__device__ __forceinline__ uint64_t smem_desc_sw32(uint32_t saddr)
+{
+    // start address >> 4 | LBO (unused for swizzled K-major) = 1 | SBO = 256 B (8 rows x 32 B)
+    // | version 1 (bits 46-47) | layout SWIZZLE_32B = 6 (bits 61-63)
+    return static_cast<uint64_t>((saddr >> 4) & 0x3FFFu) | (static_cast<uint64_t>(1) << 16) |
+           (static_cast<uint64_t>(256 >> 4) << 32) | (static_cast<uint64_t>(1) << 46) |
+           (static_cast<uint64_t>(6) << 61);
+}
+
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
+{
+    // D f32 (bits 4-5 = 1), A bf16 (7-9 = 1), B bf16 (10-12 = 1), both K-major,
+    // N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+    return (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
+           (static_cast<uint32_t>(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                 "l"(a), "l"(b), "r"(idesc), "r"(acc)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                   "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                   "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+        v[i] = __uint_as_float(r[i]);
+}
+
+// Byte offset of element (row r, column c) of a 32-byte-row K-major tile in
+// the 32B-swizzled layout.
+__host__ __device__ __forceinline__ uint32_t sw32_offset(uint32_t r, uint32_t c)
+{
+    const uint32_t chunk = (c >> 3) ^ ((r >> 2) & 1u);
+    return r * 32u + chunk * 16u + (c & 7u) * 2u;
+}
+
+// ---- plan building --------------------------------------------------------------------
+__global__ void tile_flags_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ row_ptr, int64_t m,
+                                  int64_t kb, int32_t *__restrict__ flags)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t r = warp; r < m; r += nw) {
+        const int64_t base = (r / kPanel) * kb;
+        for (int64_t e = row_ptr[r] + lane; e < row_ptr[r + 1]; e += 32)
+            flags[base + packed[e].col / kTileK] = 1;
+    }
+}
+
+__global__ void tile_list_kernel(const int32_t *__restrict__ pf, int64_t total, int64_t kb, int32_t *__restrict__ tile_cb)
+{
+    for (int64_t f = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; f < total;
+         f += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        if (pf[f + 1] != pf[f])
+            tile_cb[pf[f]] = static_cast<int32_t>(f % kb);
+}
+
+__global__ void tile_fill_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ row_ptr, int64_t m,
+                                 int64_t kb, const int32_t *__restrict__ pf, __nv_bfloat16 *__restrict__ hi,
+                                 __nv_bfloat16 *__restrict__ lo)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t r = warp; r < m; r += nw) {
+        const int64_t base = (r / kPanel) * kb;
+        const uint32_t lr = static_cast<uint32_t>(r % kPanel);
+        for (int64_t e = row_ptr[r] + lane; e < row_ptr[r + 1]; e += 32) {
+            const Entry t = packed[e];
+            const int64_t tile = pf[base + t.col / kTileK];
+            const uint32_t off = sw32_offset(lr, static_cast<uint32_t>(t.col % kTileK)) / 2;
+            const __nv_bfloat16 h = __float2bfloat16_rn(t.val);
+            hi[tile * (kTileBytes / 2) + off] = h;
+            if (lo)
+                lo[tile * (kTileBytes / 2) + off] = __float2bfloat16_rn(t.val - __bfloat162float(h));
+        }
+    }
+}
+
+// B (k x n FP32, row-major) -> tiles [jt][cb] of N rows (output columns) x 16 k, swizzled.
+__global__ void b_tiles_kernel(const float *__restrict__ B, int64_t k, int64_t n, int N, int64_t kb,
+                               __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo)
+{
+    const int64_t cb = blockIdx.x;
+    const int64_t jt = blockIdx.y;
+    const int64_t tile = jt * kb + cb;
+    const size_t tile_elems = static_cast<size_t>(N) * kTileK;
+    for (int idx = threadIdx.x; idx < N * kTileK; idx += blockDim.x) {
+        const int jj = idx % N;          // consecutive threads: consecutive columns of B (coalesced reads)
+        const int kk = idx / N;
+        const int64_t c = cb * kTileK + kk;
+        const int64_t j = jt * N + jj;
+        const float v = (c < k && j < n) ? __ldg(B + c * n + j) : 0.0f;
+        const uint32_t off = sw32_offset(static_cast<uint32_t>(jj), static_cast<uint32_t>(kk)) / 2;
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        hi[tile * tile_elems + off] = h;
+        if (lo)
+            lo[tile * tile_elems + off] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
+}
+
+// ---- the MMA kernel ---------------------------------------------------------------------
+template <int N, int S, bool SPLIT>
+struct TcCfg {
+    static constexpr int kABytes = kTileBytes * (SPLIT ? 2 : 1);
+    static constexpr int kBBytes = N * 32 * (SPLIT ? 2 : 1);
+    static constexpr int kStage = kABytes + kBBytes;
+    static constexpr int kSmem = 1024 /* barriers, tmem slot */ + S * kStage + 1024 /* alignment slack */;
+};
+
+template <int N, int S, bool SPLIT>
+__global__ void __launch_bounds__(128, 1)
+spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_cb, const uint16_t *__restrict__ a_hi,
+               const uint16_t *__restrict__ a_lo, const uint16_t *__restrict__ b_hi, const uint16_t *__restrict__ b_lo,
+               int64_t m, int64_t n, int64_t kb, float *__restrict__ C, uint32_t *__restrict__ status)
+{
+    using Cfg = TcCfg<N, S, SPLIT>;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // carve: [0,1024) control, then 1024-aligned stages
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+    uint64_t *full = reinterpret_cast<uint64_t *>(base);
+    uint64_t *empty = full + S;
+    uint64_t *done = empty + S;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    unsigned char *stages = base + 1024;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t panel = blockIdx.x;
+    const int64_t jt = blockIdx.y;
+    const int64_t t0 = pf[panel * kb];
+    const int64_t t1 = pf[(panel + 1) * kb];
+    const int64_t ntiles = t1 - t0;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == 2) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(N)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (ntiles > 0) {
+        if (warp == 0 && lane == 0) {
+            // producer
+            for (int64_t i = 0; i < ntiles; ++i) {
+                const int s = static_cast<int>(i % S);
+                if (i >= S && !mbar_wait(&empty[s], static_cast<uint32_t>(((i / S) - 1) & 1))) {
+                    atomicOr(status, kStatusWaitTimeout);
+                    *abort_flag = 1;
+                    break;
+                }
+                if (*abort_flag)
+                    break;
+                unsigned char *st = stages + static_cast<size_t>(s) * Cfg::kStage;
+                const int64_t tile = t0 + i;
+                const int64_t btile = jt * kb + tile_cb[tile];
+                mbar_arrive_expect_tx(&full[s], Cfg::kStage);
+                bulk_g2s(st, a_hi + tile * (kTileBytes / 2), kTileBytes, &full[s]);
+                bulk_g2s(st + Cfg::kABytes, b_hi + btile * (N * 16), N * 32, &full[s]);
+                if (SPLIT) {
+                    bulk_g2s(st + kTileBytes, a_lo + tile * (kTileBytes / 2), kTileBytes, &full[s]);
+                    bulk_g2s(st + Cfg::kABytes + N * 32, b_lo + btile * (N * 16), N * 32, &full[s]);
+                }
+            }
+        } else if (warp == 1 && lane == 0) {
+            // MMA issuer
+            const uint32_t idesc = idesc_bf16(kPanel, N);
+            int64_t i = 0;
+            for (; i < ntiles; ++i) {
+                const int s = static_cast<int>(i % S);
+                if (!mbar_wait(&full[s], static_cast<uint32_t>((i / S) & 1))) {
+                    atomicOr(status, kStatusWaitTimeout);
+                    *abort_flag = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t st = smem_u32(stages + static_cast<size_t>(s) * Cfg::kStage);
+                const uint64_t ah = smem_desc_sw32(st);
+                const uint64_t bh = smem_desc_sw32(st + Cfg::kABytes);
+                tc_mma(tmem, ah, bh, idesc, i > 0 ? 1u : 0u);
+                if (SPLIT) {
+                    const uint64_t al = smem_desc_sw32(st + kTileBytes);
+                    const uint64_t bl = smem_desc_sw32(st + Cfg::kABytes + N * 32);
+                    tc_mma(tmem, ah, bl, idesc, 1u);
+                    tc_mma(tmem, al, bh, idesc, 1u);
+                }
+                tc_commit(&empty[s]); // slot reusable once these MMAs have read it
+            }
+            tc_commit(done); // arrives when every MMA issued above has completed
+        }
+        __syncwarp();
+        // epilogue: all four warps (warp w owns TMEM lanes 32w..32w+31 = panel rows)
+        const bool ok = mbar_wait(done, 0);
+        if (!ok && lane == 0)
+            atomicOr(status, kStatusWaitTimeout);
+        tc_fence_after();
+        const int64_t row = panel * kPanel + warp * 32 + lane;
+        if (__all_sync(0xffffffffu, ok ? 1 : 0) && !*abort_flag) {
+#pragma unroll 1
+            for (int c = 0; c < N; c += 32) {
+                float v[32];
+                tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c), v);
+                const int64_t j = jt * N + c;
+                if (row < m && j < n) {
+                    float *out = C + row * n + j;
+                    if (j + 32 <= n) {
+#pragma unroll
+                        for (int q = 0; q < 32; q += 4)
+                            *reinterpret_cast<float4 *>(out + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 32; ++q)
+                            if (j + q < n)
+                                out[q] = v[q];
+                    }
+                }
+            }
+        }
+        // the producer's copies in flight must land before the CTA exits
+        if (*abort_flag && threadIdx.x == 0) {
+            for (int s = 0; s < S; ++s)
+                mbar_wait(&full[s], 0);
+        }
+    } else {
+        // panel without entries: C rows are zero
+        const int64_t row = panel * kPanel + warp * 32 + lane;
+        if (row < m)
+            for (int64_t j = jt * N; j < (jt + 1) * N && j < n; ++j)
+                C[row * n + j] = 0.0f;
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 2) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(N) : "memory");
+    }
+}
+
+int tile_n_for(int64_t n) { return n >= 256 ? 256 : 128; }
+
+template <int N, int S, bool SPLIT>
+cudaError_t launch_tc(const TcPlan &p, int64_t m, int64_t n, float *C, uint32_t *status, cudaStream_t st)
+{
+    using Cfg = TcCfg<N, S, SPLIT>;
+    auto kern = spdm_tc_kernel<N, S, SPLIT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::kSmem);
+    if (e != cudaSuccess)
+        return e;
+    dim3 grid(static_cast<unsigned>(p.panels), static_cast<unsigned>((n + N - 1) / N));
+    kern<<<grid, 128, Cfg::kSmem, st>>>(p.pf.ptr, p.tile_cb.ptr, p.a_hi.ptr, p.a_lo.ptr, p.b_hi.ptr, p.b_lo.ptr, m, n,
+                                        p.kb, C, status);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+// Builds the densified tile plan (one synchronisation to size the tiles).
+gcoo_status tc_build_plan(gcoo_handle *h, bool split, cudaStream_t st)
+{
+    if (h->tc && h->tc->split == split && h->tc->nnz == h->nnz)
+        return GCOO_SUCCESS;
+    destroy_tc_plan(h->tc);
+    h->tc = new (std::nothrow) TcPlan();
+    if (!h->tc)
+        return fail(GCOO_ERROR_ALLOC, "host allocation failed");
+    TcPlan &p = *h->tc;
+    p.split = split;
+    p.nnz = h->nnz;
+    p.panels = (h->m + kPanel - 1) / kPanel;
+    p.kb = (h->k + kTileK - 1) / kTileK;
+    const int64_t L = p.panels * p.kb;
+    const size_t sc = scan_scratch_elems(L);
+    if (!p.pf.ensure(L + 1) || !p.scratch.ensure(sc + 1))
+        return fail(GCOO_ERROR_ALLOC, "device allocation of the tile plan failed");
+    GCOO_CUDA(cudaMemsetAsync(p.pf.ptr, 0, sizeof(int32_t) * (L + 1), st));
+    unsigned blocks = static_cast<unsigned>(std::min<int64_t>((h->m + 7) / 8, 152 * 16));
+    tile_flags_kernel<<<blocks, 256, 0, st>>>(h->packed.ptr, h->row_ptr.ptr, h->m, p.kb, p.pf.ptr);
+    count_launches(1);
+    GCOO_LAUNCH("tile_flags_kernel");
+    GCOO_CUDA(launch_row_scan(p.pf.ptr, L, 1, nullptr, nullptr, p.scratch.ptr + sc, p.scratch.ptr, nullptr, st));
+    int64_t total = 0;
+    GCOO_CUDA(cudaMemcpyAsync(&total, p.scratch.ptr + sc, sizeof(total), cudaMemcpyDeviceToHost, st));
+    GCOO_CUDA(cudaStreamSynchronize(st));
+    p.tiles = total;
+    const size_t tile_elems = static_cast<size_t>(kTileBytes / 2);
+    if (!p.tile_cb.ensure(total + 1) || !p.a_hi.ensure(total * tile_elems + 1) ||
+        (split && !p.a_lo.ensure(total * tile_elems + 1)))
+        return fail(GCOO_ERROR_ALLOC, "device allocation of the dense tiles failed");
+    if (total > 0) {
+        tile_list_kernel<<<static_cast<unsigned>(std::min<int64_t>((L + 255) / 256, 4096)), 256, 0, st>>>(p.pf.ptr, L,
+                                                                                                          p.kb, p.tile_cb.ptr);
+        GCOO_CUDA(cudaMemsetAsync(p.a_hi.ptr, 0, total * kTileBytes, st));
+        if (split)
+            GCOO_CUDA(cudaMemsetAsync(p.a_lo.ptr, 0, total * kTileBytes, st));
+        tile_fill_kernel<<<blocks, 256, 0, st>>>(h->packed.ptr, h->row_ptr.ptr, h->m, p.kb, p.pf.ptr,
+                                                 reinterpret_cast<__nv_bfloat16 *>(p.a_hi.ptr),
+                                                 split ? reinterpret_cast<__nv_bfloat16 *>(p.a_lo.ptr) : nullptr);
+        count_launches(2);
+        GCOO_LAUNCH("tile plan kernels");
+    }
+    return GCOO_SUCCESS;
+}
+
+// Density of the stored tiles (entries / tile slots); 0 before a plan exists.
+double tc_density(const gcoo_handle *h)
+{
+    if (!h->tc || h->tc->tiles == 0)
+        return 0.0;
+    return static_cast<double>(h->nnz) / (static_cast<double>(h->tc->tiles) * kPanel * kTileK);
+}
+
+gcoo_status tc_prepare_b(gcoo_handle *h, int64_t n)
+{
+    TcPlan &p = *h->tc;
+    const int N = tile_n_for(n);
+    const int64_t nt = (n + N - 1) / N;
+    const size_t elems = static_cast<size_t>(nt) * p.kb * N * kTileK;
+    if (!p.b_hi.ensure(elems) || (p.split && !p.b_lo.ensure(elems)))
+        return fail(GCOO_ERROR_ALLOC, "device allocation of the B tiles failed");
+    p.b_n = n;
+    return GCOO_SUCCESS;
+}
+
+gcoo_status tc_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, cudaStream_t st)
+{
+    TcPlan &p = *h->tc;
+    const int N = tile_n_for(n);
+    dim3 g(static_cast<unsigned>(p.kb), static_cast<unsigned>((n + N - 1) / N));
+    b_tiles_kernel<<<g, 256, 0, st>>>(dB, h->k, n, N, p.kb, reinterpret_cast<__nv_bfloat16 *>(p.b_hi.ptr),
+                                      p.split ? reinterpret_cast<__nv_bfloat16 *>(p.b_lo.ptr) : nullptr);
+    count_launches(1);
+    GCOO_LAUNCH("b_tiles_kernel");
+    cudaError_t e;
+    if (N == 256)
+        e = p.split ? launch_tc<256, 6, true>(p, h->m, n, dC, h->status.ptr, st)
+                    : launch_tc<256, 8, false>(p, h->m, n, dC, h->status.ptr, st);
+    else
+        e = p.split ? launch_tc<128, 8, true>(p, h->m, n, dC, h->status.ptr, st)
+                    : launch_tc<128, 12, false>(p, h->m, n, dC, h->status.ptr, st);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "spdm_tc_kernel launch");
+    return GCOO_SUCCESS;
+}
+
+} // namespace gcoo

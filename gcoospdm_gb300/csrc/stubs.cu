@@ -1,11 +1,6 @@
-// temporary: forms, batch and autotune not yet built
+// temporary: batch and autotune not yet built
 #include "handle.hpp"
 namespace gcoo {
-void destroy_tc_plan(TcPlan *) {}
-void destroy_lowp_work(LowpWork *) {}
-gcoo_status run_form(gcoo_handle *, const float *, int64_t, float *, gcoo_precision, cudaStream_t, bool)
-{ return fail(GCOO_ERROR_UNSUPPORTED, "form not built yet"); }
-bool form_uses_tensor(gcoo_handle *, gcoo_precision) { return false; }
 bool tuned_params(int64_t, int64_t, int64_t, int64_t, gcoo_params *) { return false; }
 }
 extern "C" {
