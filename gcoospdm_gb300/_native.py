@@ -31,7 +31,7 @@ EXPORTS = (
     "gcoo_set_allocator", "gcoo_create", "gcoo_build", "gcoo_export", "gcoo_spdm", "gcoo_spdm_ex",
     "gcoo_prepare", "gcoo_multiply_by", "gcoo_destroy", "gcoo_query_engine", "gcoo_kernel_launches",
     "gcoo_device_status",
-    "gcoo_convert_count", "gcoo_convert_scatter", "gcoo_spdm_view", "gcoo_error_norm",
+    "gcoo_convert_count", "gcoo_convert_count_static", "gcoo_convert_scatter", "gcoo_spdm_view", "gcoo_error_norm",
     "gcoo_batch_create", "gcoo_batch_run", "gcoo_batch_launches", "gcoo_batch_destroy",
     "gcoo_autotune", "gcoo_autotune_save", "gcoo_autotune_load", "gcoo_autotune_clear",
 )
@@ -98,6 +98,7 @@ def _declare(L) -> None:
         "gcoo_kernel_launches": (C.c_uint64, []),
         "gcoo_device_status": (st, [vp, vp, C.POINTER(C.c_uint32)]),
         "gcoo_convert_count": (st, [vp, i64, i64, i32, vp, vp, C.POINTER(i64), vp]),
+        "gcoo_convert_count_static": (st, [vp, i64, i64, i32, vp, vp, C.POINTER(i64), vp]),
         "gcoo_convert_scatter": (st, [vp, i64, i64, i32, vp, vp, vp, vp, vp]),
         "gcoo_spdm_view": (st, [C.POINTER(View), vp, i64, vp, vp]),
         "gcoo_error_norm": (st, [vp, vp, i64, vp, C.POINTER(C.c_double), vp]),

@@ -167,6 +167,20 @@ gcoo_status gcoo_convert_count(const float *dA, int64_t m, int64_t k, int32_t ro
                                int32_t *d_group_index, int32_t *d_nnz_per_group, int64_t *nnz,
                                void *stream);
 
+/* No counterpart in the reference. Same count + scan and same results as
+ * gcoo_convert_count, for callers that cannot allocate device memory when
+ * they convert (memory owned by another runtime's pool, loops that must not
+ * pay cudaMalloc's implicit synchronisation, bindings without an allocator):
+ * it allocates nothing and keeps its per-row counts and block sums in a
+ * fixed ~4.2 MB __device__ array held by every GPU that loads the library.
+ * Limit: m <= 2^20 rows (larger m -> GCOO_ERROR_INVALID_VALUE). The first
+ * call on a device looks up that array's address: make it before any stream
+ * capture. All calls share the array, so calls that overlap on the GPU race.
+ * Synchronises `stream` to return *nnz. */
+gcoo_status gcoo_convert_count_static(const float *dA, int64_t m, int64_t k, int32_t rows_per_group,
+                                      int32_t *d_group_index, int32_t *d_nnz_per_group, int64_t *nnz,
+                                      void *stream);
+
 /* Stable scatter of convertToGroupCOOFormat (src/ShGCOOSpDM.cu:94-111,
  * src/gcoo_spdm_kernels.cu:30-90) into caller arrays of at least nnz
  * entries, using a group_index produced by gcoo_convert_count. */
