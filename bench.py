@@ -45,7 +45,45 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the extra precision/batched lines")
+    ap.add_argument("--sweep", action="store_true", help="print the FP32 n x sparsity sweep instead")
+    ap.add_argument("--case", choices=["tc_bf16", "tc_split", "convert", "fp32", "batched", "fp8", "bf16_fma"],
+                    help="run one small case a few times (for profiling) and exit")
     return ap.parse_args()
+
+
+def run_case(args):
+    """A few launches of one kernel on a small case (sized for ncu captures)."""
+    import torch
+    import gcoospdm_gb300 as g
+    from gcoospdm_gb300 import datagen as dg
+    dev = torch.device("cuda", 0)
+    if args.case in ("tc_bf16", "tc_split"):
+        m, n = 8192, 1024
+        A = dg.block_dense_torch(4096 + 750, m, m, 0.25, device=dev)
+        B = dg.dense_pm1_torch(4096, 5, m, n, device=dev)
+        h = g.GcooHandle(A).build()
+        prec = "bf16" if args.case == "tc_bf16" else "split_bf16"
+        for _ in range(3):
+            h.spdm(B, prec=prec)
+    elif args.case == "batched":
+        res = run_batched(g, dg, torch, dev, count=64)
+        print(json.dumps(res))
+    else:
+        n = args.n
+        A = dg.bernoulli_dense_torch(SEED, n, n, 1.0 - args.sparsity, device=dev)
+        B = dg.dense_pm1_torch(SEED, 5, n, n, device=dev)
+        h = g.GcooHandle(A).build()
+        for _ in range(3):
+            if args.case == "convert":
+                h.build()
+            elif args.case == "fp32":
+                h.spdm(B)
+            elif args.case == "fp8":
+                h.spdm(B, prec="fp8_b")
+            else:
+                h.spdm(B, prec="bf16")
+    torch.cuda.synchronize()
+    print(f"case {args.case} done", flush=True)
 
 
 def dist_setup(gpus):
@@ -354,15 +392,157 @@ def run_ours(args, rank, world, local, pg):
     print(json.dumps(line), flush=True)
 
 
+def _time(torch, fn, reps=5, warm=2):
+    stream = torch.cuda.current_stream()
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps  # ms
+
+
+def _rel_fro_rows(torch, A, B, C, rows):
+    """Relative Frobenius error of C on sampled rows against an FP64 product."""
+    idx = torch.as_tensor(rows, device=A.device)
+    ref = A[idx].double() @ B.double()
+    return float(torch.linalg.norm(C[idx].double() - ref) / torch.linalg.norm(ref))
+
+
+def run_precision_forms(g, dg, torch, dev, sparsities=(0.5, 0.75, 0.9), m=8192, n=1024):
+    """Block-clustered A (16x16 blocks), every form, time + error vs FP64."""
+    out = {}
+    B = dg.dense_pm1_torch(4096, 5, m, n, device=dev)
+    sample = list(range(0, m, 97))
+    for s in sparsities:
+        A = dg.block_dense_torch(4096 + int(s * 1000), m, m, 1.0 - s, device=dev)
+        h = g.GcooHandle(A).build()
+        nnz = h.nnz
+        flop = 2.0 * nnz * n
+        Cd = torch.empty(m, n, device=dev)
+        row = {"nnz": nnz}
+        for prec in ("fp32", "bf16", "split_bf16", "fp8_b"):
+            h.prepare(n, prec)
+            ms = _time(torch, lambda: h.spdm(B, Cd, prec=prec))
+            row[prec] = {"ms": round(ms, 4), "gflops": round(flop / ms / 1e6, 1),
+                         "rel_fro_vs_fp64": _rel_fro_rows(torch, A, B, Cd, sample),
+                         "engine": "tensor" if (prec != "fp32" and h.query_engine(prec)) else "fma"}
+        row["bf16_speedup_vs_fp32"] = round(row["fp32"]["ms"] / row["bf16"]["ms"], 2)
+        row["split_speedup_vs_fp32"] = round(row["fp32"]["ms"] / row["split_bf16"]["ms"], 2)
+        out[f"s{s}"] = row
+        del A, h, Cd
+        torch.cuda.empty_cache()
+    return {"workload": f"A {m}x{m} 16x16 block mask, B {m}x{n}", **out}
+
+
+def run_batched(g, dg, torch, dev, count=512):
+    """512 independent multiplies: sequential FP32 launches vs one persistent launch."""
+    shapes = dg.batched_shapes(5120, count)
+    probs = []
+    flop = 0.0
+    for i, (m, k, n, s) in enumerate(shapes):
+        A = dg.bernoulli_dense_torch(6000 + i, m, k, 1.0 - s, device=dev)
+        B = dg.dense_pm1_torch(6000 + i, 5, k, n, device=dev)
+        h = g.GcooHandle(A).build()
+        C = torch.empty(m, n, device=dev)
+        probs.append((h, A, B, C))
+        flop += 2.0 * h.nnz * n
+    seq_ms = _time(torch, lambda: [h.spdm(B, C) for h, A, B, C in probs], reps=3, warm=1)
+    res = {"workload": f"{count} problems, m,k U[256,4096], n in {{32,64,128}}, s U[0.9,0.999]",
+           "gflop": round(flop / 1e9, 3), "sequential_fp32": {"ms": round(seq_ms, 4), "launches": count,
+                                                              "gflops": round(flop / seq_ms / 1e6, 1)}}
+    refs = [C.clone() for h, A, B, C in probs[:16]]
+    L = g.lib()
+    for prec in ("fp32", "bf16"):
+        bt = g.GcooBatch([(h, B, C) for h, A, B, C in probs], prec=prec)
+        l0 = L.gcoo_kernel_launches()
+        ms = _time(torch, bt.run, reps=10, warm=2)
+        launches = (L.gcoo_kernel_launches() - l0) // 12
+        errs = [_rel_fro_rows(torch, A, B, C, list(range(0, A.shape[0], 7))) for h, A, B, C in probs[:16]]
+        same = all(torch.equal(C, r) for (h, A, B, C), r in zip(probs[:16], refs)) if prec == "fp32" else None
+        res[f"batched_{prec}"] = {"ms": round(ms, 4), "gflops": round(flop / ms / 1e6, 1), "launches": int(launches),
+                                  "speedup_vs_sequential_fp32": round(seq_ms / ms, 2),
+                                  "max_rel_fro_vs_fp64": max(errs), "bit_identical_to_single": same}
+        bt.close()
+    return res
+
+
+def run_irregular(g, dg, torch, dev, m=65536, n=256, nnz=1_200_000):
+    """Zipf(2) row counts capped at 4096, 65536^2 sparse operand (dense: 17 GB)."""
+    rows, cols, vals = dg.zipf_coo(65536, m, m, nnz, alpha=2.0, cap=4096)
+    A = torch.zeros(m, m, device=dev)
+    A[torch.from_numpy(rows).to(dev), torch.from_numpy(cols).to(dev)] = torch.from_numpy(vals).to(dev)
+    B = dg.normal_dense(65536, 40, m, n)
+    B = torch.from_numpy(B).to(dev)
+    h = g.GcooHandle(A)
+    conv_ms = _time(torch, h.build, reps=3, warm=1)
+    Cd = torch.empty(m, n, device=dev)
+    ms = _time(torch, lambda: h.spdm(B, Cd), reps=10)
+    err = h.error_norm(B, Cd)
+    flop = 2.0 * h.nnz * n
+    counts = torch.bincount(torch.from_numpy(rows), minlength=m)
+    res = {"workload": f"A {m}x{m} Zipf(2) rows capped 4096, nnz {h.nnz}, B {m}x{n} N(0,1)",
+           "max_row_nnz": int(counts.max()), "convert_ms": round(conv_ms, 4), "spdm_ms": round(ms, 4),
+           "gflops": round(flop / ms / 1e6, 1), "rel_fro_vs_fp64": err,
+           "spdm_gbps": round((12 * h.nnz + 8 * (m // 4 + 1) + 4 * m * n * 2) / ms / 1e6, 1)}
+    del A
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_forms(args, g, dg, torch, dev):
-    """Extra measurements of the other arithmetic forms (filled as they land)."""
-    return None
+    """Extra measurements: precision forms, batched, irregular."""
+    out = {}
+    for name, fn in (("precision_forms", lambda: run_precision_forms(g, dg, torch, dev)),
+                     ("batched", lambda: run_batched(g, dg, torch, dev)),
+                     ("irregular", lambda: run_irregular(g, dg, torch, dev))):
+        try:
+            out[name] = fn()
+        except Exception as e:  # report, never hide: the main line still prints
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        torch.cuda.empty_cache()
+    return out
+
+
+def run_sweep(args):
+    """The FP32 sweep (n x sparsity grid): one JSON line per point."""
+    import torch
+    import gcoospdm_gb300 as g
+    from gcoospdm_gb300 import datagen as dg
+    dev = torch.device("cuda", 0)
+    for n in (2048, 4096, 8192, 16384):
+        B = dg.dense_pm1_torch(n, 5, n, n, device=dev)
+        Cd = torch.empty(n, n, device=dev)
+        for s in (0.95, 0.98, 0.99, 0.995, 0.999):
+            A = dg.bernoulli_dense_torch(n + int(s * 1e4), n, n, 1.0 - s, device=dev)
+            h = g.GcooHandle(A)
+            conv = _time(torch, h.build, reps=3, warm=1)
+            ms = _time(torch, lambda: h.spdm(B, Cd), reps=5)
+            e2e = _time(torch, lambda: h.multiply_by(B, Cd), reps=3)
+            nnz = h.nnz
+            alg = 12 * nnz + 8 * (n // 4 + 1) + 8 * n * n
+            print(json.dumps({"n": n, "sparsity": s, "nnz": nnz, "convert_ms": round(conv, 4),
+                              "spdm_ms": round(ms, 4), "spdm_gflops": round(2.0 * nnz * n / ms / 1e6, 1),
+                              "spdm_gbps": round(alg / ms / 1e6, 1), "multiply_by_ms": round(e2e, 4),
+                              "multiply_by_gflops": round(2.0 * nnz * n / e2e / 1e6, 1),
+                              "rel_fro_vs_fp64": h.error_norm(B, Cd) if n <= 4096 else None}), flush=True)
+            del A, h
+        del B, Cd
+        torch.cuda.empty_cache()
 
 
 def main():
     args = parse()
     rank, world, local, pg = dist_setup(args.gpus)
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+    elif args.sweep:
+        run_sweep(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world, local, pg)

@@ -1,0 +1,461 @@
+// batched.cu -- many independent multiplies in one persistent launch.
+//
+// gcoo_batch_create turns each problem (a built handle, its B, its C) into
+// work items of `rows_per_item` consecutive rows at full width, sorts all
+// items by their entry count (descending, so the longest items start first)
+// into a device queue, and captures [queue reset, (B -> BF16), persistent
+// kernel] into a CUDA graph on a private stream. gcoo_batch_run replays that
+// graph on the caller's stream: one kernel launch (two for BF16) whatever the
+// number of problems. CTAs of the persistent kernel pull items with an atomic
+// counter (no waits on other CTAs); each warp computes whole rows of an item
+// with the same sequential fmaf chain as the single-problem kernels, so FP32
+// results are bit-identical to gcoo_spdm per problem and BF16 results to
+// gcoo_spdm_ex(BF16) on the FMA engine.
+//
+// rows_per_item is chosen per shape bucket (n and density class) by timing
+// the candidates on that bucket's items (the autotune table, persisted with
+// gcoo_autotune_save); a loaded table skips the timing.
+#include <cuda_bf16.h>
+#include <math.h>
+
+#include <algorithm>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "handle.hpp"
+
+namespace gcoo {
+
+struct BatchProb {
+    const Entry *packed;
+    const int32_t *row_ptr;
+    const float *B;
+    const uint16_t *Bbf;
+    float *C;
+    int64_t n;
+};
+
+struct BatchItem {
+    int32_t prob, row0, row1, vec;
+};
+
+struct ConvSeg {
+    const float *src;
+    uint16_t *dst;
+    int64_t count4;
+};
+
+} // namespace gcoo
+
+struct gcoo_batch {
+    gcoo_precision prec = GCOO_PREC_FP32;
+    int32_t count = 0;
+    std::vector<gcoo_problem> probs;
+    std::vector<std::vector<int32_t>> row_ptr_h;
+    std::vector<std::string> bucket;
+    std::vector<int> vec;
+    gcoo::DevBuf<gcoo::BatchProb> d_probs;
+    gcoo::DevBuf<gcoo::BatchItem> d_items;
+    gcoo::DevBuf<unsigned> counter;
+    gcoo::DevBuf<uint16_t> bf_ws;
+    gcoo::DevBuf<gcoo::ConvSeg> d_segs;
+    int nitems = 0;
+    int grid = 0;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~gcoo_batch()
+    {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        if (graph)
+            cudaGraphDestroy(graph);
+        if (cap)
+            cudaStreamDestroy(cap);
+    }
+};
+
+namespace gcoo {
+
+namespace {
+
+constexpr int kBatchThreads = 256;
+
+template <int V, bool BF16>
+struct BLoad;
+template <int V>
+struct BLoad<V, false> {
+    static __device__ __forceinline__ void load(const BatchProb &p, int64_t off, float (&b)[V])
+    {
+        if constexpr (V == 4) {
+            const float4 t = __ldg(reinterpret_cast<const float4 *>(p.B + off));
+            b[0] = t.x; b[1] = t.y; b[2] = t.z; b[3] = t.w;
+        } else if constexpr (V == 2) {
+            const float2 t = __ldg(reinterpret_cast<const float2 *>(p.B + off));
+            b[0] = t.x; b[1] = t.y;
+        } else {
+            b[0] = __ldg(p.B + off);
+        }
+    }
+};
+template <int V>
+struct BLoad<V, true> {
+    static __device__ __forceinline__ void load(const BatchProb &p, int64_t off, float (&b)[V])
+    {
+        if constexpr (V == 4) {
+            const uint2 t = __ldg(reinterpret_cast<const uint2 *>(p.Bbf + off));
+            b[0] = __uint_as_float(t.x << 16); b[1] = __uint_as_float(t.x & 0xffff0000u);
+            b[2] = __uint_as_float(t.y << 16); b[3] = __uint_as_float(t.y & 0xffff0000u);
+        } else if constexpr (V == 2) {
+            const uint32_t t = __ldg(reinterpret_cast<const unsigned int *>(p.Bbf + off));
+            b[0] = __uint_as_float(t << 16); b[1] = __uint_as_float(t & 0xffff0000u);
+        } else {
+            b[0] = __uint_as_float(static_cast<uint32_t>(__ldg(reinterpret_cast<const unsigned short *>(p.Bbf + off))) << 16);
+        }
+    }
+};
+
+template <int V, bool BF16>
+__device__ __forceinline__ void item_rows(const BatchProb &p, int row0, int row1, int warp, int lane)
+{
+    constexpr int W = kBatchThreads / 32;
+    for (int row = row0 + warp; row < row1; row += W) {
+        const int64_t e0 = p.row_ptr[row], e1 = p.row_ptr[row + 1];
+        for (int64_t j = static_cast<int64_t>(lane) * V; j < p.n; j += 32 * V) {
+            float acc[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                acc[v] = 0.0f;
+            int64_t e = e0;
+#pragma unroll 1
+            for (; e + 4 <= e1; e += 4) {
+                Entry t[4];
+                float b[4][V];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    t[u] = p.packed[e + u];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    BLoad<V, BF16>::load(p, static_cast<int64_t>(t[u].col) * p.n + j, b[u]);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float a = BF16 ? __bfloat162float(__float2bfloat16_rn(t[u].val)) : t[u].val;
+#pragma unroll
+                    for (int v = 0; v < V; ++v)
+                        acc[v] = fmaf(a, b[u][v], acc[v]);
+                }
+            }
+#pragma unroll 1
+            for (; e < e1; ++e) {
+                const Entry t = p.packed[e];
+                float b[V];
+                BLoad<V, BF16>::load(p, static_cast<int64_t>(t.col) * p.n + j, b);
+                const float a = BF16 ? __bfloat162float(__float2bfloat16_rn(t.val)) : t.val;
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    acc[v] = fmaf(a, b[v], acc[v]);
+            }
+            float *out = p.C + static_cast<int64_t>(row) * p.n + j;
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                out[v] = acc[v];
+        }
+    }
+}
+
+// Persistent: CTAs pull work items from the queue with an atomic counter.
+template <bool BF16>
+__global__ void __launch_bounds__(kBatchThreads)
+batch_kernel(const BatchProb *__restrict__ probs, const BatchItem *__restrict__ items, int nitems,
+             unsigned *__restrict__ counter)
+{
+    __shared__ int s_item;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (;;) {
+        __syncthreads(); // everyone has read the previous item index
+        if (threadIdx.x == 0)
+            s_item = static_cast<int>(atomicAdd(counter, 1u));
+        __syncthreads();
+        const int it = s_item;
+        if (it >= nitems)
+            break;
+        const BatchItem w = items[it];
+        const BatchProb p = probs[w.prob];
+        if (w.vec == 4)
+            item_rows<4, BF16>(p, w.row0, w.row1, warp, lane);
+        else if (w.vec == 2)
+            item_rows<2, BF16>(p, w.row0, w.row1, warp, lane);
+        else
+            item_rows<1, BF16>(p, w.row0, w.row1, warp, lane);
+    }
+}
+
+__global__ void batch_bf16_kernel(const ConvSeg *__restrict__ segs)
+{
+    const ConvSeg s = segs[blockIdx.y];
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < s.count4;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const float4 v = __ldcs(reinterpret_cast<const float4 *>(s.src) + i);
+        const __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y);
+        const __nv_bfloat162 b = __floats2bfloat162_rn(v.z, v.w);
+        reinterpret_cast<uint2 *>(s.dst)[i] =
+            make_uint2(*reinterpret_cast<const uint32_t *>(&a), *reinterpret_cast<const uint32_t *>(&b));
+    }
+}
+
+int pick_vec(int64_t n, const float *B, const float *C)
+{
+    const uintptr_t a = reinterpret_cast<uintptr_t>(B) | reinterpret_cast<uintptr_t>(C);
+    if (n >= 128 && n % 4 == 0 && (a & 15) == 0)
+        return 4;
+    if (n >= 64 && n % 2 == 0 && (a & 7) == 0)
+        return 2;
+    return 1;
+}
+
+std::string batch_bucket(const gcoo_problem &p)
+{
+    const gcoo_handle *h = p.a;
+    const double density = static_cast<double>(h->nnz) / (static_cast<double>(h->m) * h->k);
+    const int d = density > 0.0 ? static_cast<int>(floor(-log2(density))) : 99;
+    int ln = 0;
+    while ((int64_t(1) << ln) < p.n)
+        ++ln;
+    return "batch_n" + std::to_string(ln) + "_d" + std::to_string(d);
+}
+
+void make_items(const gcoo_batch &b, const std::vector<int> &probs, const std::map<std::string, int> &rpi,
+                std::vector<BatchItem> &items)
+{
+    std::vector<std::pair<int64_t, BatchItem>> tmp;
+    for (int i : probs) {
+        const int r = rpi.at(b.bucket[i]);
+        const std::vector<int32_t> &rp = b.row_ptr_h[i];
+        const int m = static_cast<int>(rp.size()) - 1;
+        for (int r0 = 0; r0 < m; r0 += r) {
+            const int r1 = std::min(m, r0 + r);
+            BatchItem it{i, r0, r1, b.vec[i]};
+            tmp.push_back({static_cast<int64_t>(rp[r1] - rp[r0]) * b.probs[i].n + (r1 - r0), it});
+        }
+    }
+    std::stable_sort(tmp.begin(), tmp.end(), [](const auto &x, const auto &y) { return x.first > y.first; });
+    items.clear();
+    for (auto &t : tmp)
+        items.push_back(t.second);
+}
+
+gcoo_status upload_items(gcoo_batch &b, const std::vector<BatchItem> &items, cudaStream_t st)
+{
+    if (!b.d_items.ensure(items.size() + 1))
+        return fail(GCOO_ERROR_ALLOC, "device allocation of the work queue failed");
+    if (!items.empty())
+        GCOO_CUDA(cudaMemcpyAsync(b.d_items.ptr, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice, st));
+    b.nitems = static_cast<int>(items.size());
+    return GCOO_SUCCESS;
+}
+
+void launch_batch(const gcoo_batch &b, cudaStream_t st)
+{
+    if (b.prec == GCOO_PREC_BF16)
+        batch_kernel<true><<<b.grid, kBatchThreads, 0, st>>>(b.d_probs.ptr, b.d_items.ptr, b.nitems, b.counter.ptr);
+    else
+        batch_kernel<false><<<b.grid, kBatchThreads, 0, st>>>(b.d_probs.ptr, b.d_items.ptr, b.nitems, b.counter.ptr);
+    count_launches(1);
+}
+
+} // namespace
+} // namespace gcoo
+
+using namespace gcoo;
+
+extern "C" {
+
+gcoo_status gcoo_batch_create(gcoo_batch **out, const gcoo_problem *problems, int32_t count, gcoo_precision prec,
+                              void *stream)
+{
+    if (!out || !problems || count <= 0)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL argument or empty batch");
+    *out = nullptr;
+    if (prec != GCOO_PREC_FP32 && prec != GCOO_PREC_BF16)
+        return fail(GCOO_ERROR_UNSUPPORTED, "batched forms: GCOO_PREC_FP32 or GCOO_PREC_BF16");
+    for (int32_t i = 0; i < count; ++i) {
+        const gcoo_problem &p = problems[i];
+        if (!p.a || !p.dB || !p.dC || p.n <= 0 || p.n >= (int64_t(1) << 31))
+            return fail(GCOO_ERROR_INVALID_VALUE, "problem " + std::to_string(i) + " is incomplete");
+        if (!p.a->built)
+            return fail(GCOO_ERROR_NOT_BUILT, "problem " + std::to_string(i) + " is not built");
+        if (prec == GCOO_PREC_BF16 && ((p.a->k * p.n) % 4 != 0 || (reinterpret_cast<uintptr_t>(p.dB) & 15)))
+            return fail(GCOO_ERROR_UNSUPPORTED, "BF16 batch needs k*n % 4 == 0 and 16-byte aligned B");
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    gcoo_batch *b = new (std::nothrow) gcoo_batch();
+    if (!b)
+        return fail(GCOO_ERROR_ALLOC, "host allocation failed");
+    b->prec = prec;
+    b->count = count;
+    b->probs.assign(problems, problems + count);
+    b->row_ptr_h.resize(count);
+    b->bucket.resize(count);
+    b->vec.resize(count);
+    auto bail = [&](gcoo_status s) {
+        delete b;
+        return s;
+    };
+    // device problem table, BF16 workspace
+    std::vector<BatchProb> hp(count);
+    std::vector<ConvSeg> segs;
+    std::vector<int64_t> bf_off(count, 0);
+    int64_t bf_total = 0;
+    for (int32_t i = 0; i < count; ++i) {
+        const gcoo_problem &p = problems[i];
+        b->vec[i] = pick_vec(p.n, p.dB, p.dC);
+        b->bucket[i] = batch_bucket(p);
+        if (prec == GCOO_PREC_BF16) {
+            bf_off[i] = bf_total;
+            bf_total += (p.a->k * p.n + 15) / 16 * 16;
+        }
+    }
+    if (prec == GCOO_PREC_BF16 && !b->bf_ws.ensure(static_cast<size_t>(bf_total)))
+        return bail(fail(GCOO_ERROR_ALLOC, "device allocation of the BF16 workspace failed"));
+    for (int32_t i = 0; i < count; ++i) {
+        const gcoo_problem &p = problems[i];
+        hp[i] = BatchProb{p.a->packed.ptr, p.a->row_ptr.ptr, p.dB, prec == GCOO_PREC_BF16 ? b->bf_ws.ptr + bf_off[i] : nullptr,
+                          p.dC, p.n};
+        if (prec == GCOO_PREC_BF16)
+            segs.push_back(ConvSeg{p.dB, b->bf_ws.ptr + bf_off[i], p.a->k * p.n / 4});
+        b->row_ptr_h[i].resize(p.a->m + 1);
+    }
+    if (!b->d_probs.ensure(count) || !b->counter.ensure(1) || (prec == GCOO_PREC_BF16 && !b->d_segs.ensure(segs.size())))
+        return bail(fail(GCOO_ERROR_ALLOC, "device allocation of the batch tables failed"));
+    cudaError_t e = cudaMemcpyAsync(b->d_probs.ptr, hp.data(), sizeof(BatchProb) * count, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !segs.empty())
+        e = cudaMemcpyAsync(b->d_segs.ptr, segs.data(), sizeof(ConvSeg) * segs.size(), cudaMemcpyHostToDevice, st);
+    for (int32_t i = 0; i < count && e == cudaSuccess; ++i)
+        e = cudaMemcpyAsync(b->row_ptr_h[i].data(), problems[i].a->row_ptr.ptr, sizeof(int32_t) * (problems[i].a->m + 1),
+                            cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return bail(cuda_fail(e, "batch table upload"));
+    int per_sm = 0, dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (prec == GCOO_PREC_BF16)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<true>, kBatchThreads, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<false>, kBatchThreads, 0);
+    b->grid = std::max(1, sms) * std::max(1, per_sm);
+
+    if (prec == GCOO_PREC_BF16) { // the tuning runs below read the BF16 copy of B
+        batch_bf16_kernel<<<dim3(64, static_cast<unsigned>(segs.size())), 256, 0, st>>>(b->d_segs.ptr);
+        count_launches(1);
+    }
+    // rows_per_item per shape bucket: from the table, else timed on the bucket's items
+    std::map<std::string, std::vector<int>> by_bucket;
+    for (int32_t i = 0; i < count; ++i)
+        by_bucket[b->bucket[i]].push_back(i);
+    std::map<std::string, int> rpi;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (auto &kv : by_bucket) {
+        const std::string key = kv.first + (prec == GCOO_PREC_BF16 ? "_bf16" : "_fp32");
+        TuneEntry te;
+        if (tune_lookup(key, &te) && te.rows_per_item > 0) {
+            rpi[kv.first] = te.rows_per_item;
+            continue;
+        }
+        float best = 1e30f;
+        int best_r = 16;
+        for (int r : {4, 8, 16, 32, 64}) {
+            std::map<std::string, int> one = {{kv.first, r}};
+            std::vector<BatchItem> items;
+            make_items(*b, kv.second, one, items);
+            if (upload_items(*b, items, st) != GCOO_SUCCESS)
+                return bail(GCOO_ERROR_ALLOC);
+            float ms_min = 1e30f;
+            for (int rep = 0; rep < 3; ++rep) {
+                cudaMemsetAsync(b->counter.ptr, 0, sizeof(unsigned), st);
+                cudaEventRecord(e0, st);
+                launch_batch(*b, st);
+                cudaEventRecord(e1, st);
+                cudaEventSynchronize(e1);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                ms_min = std::min(ms_min, ms);
+            }
+            if (ms_min < best) {
+                best = ms_min;
+                best_r = r;
+            }
+        }
+        rpi[kv.first] = best_r;
+        te = TuneEntry();
+        te.rows_per_item = best_r;
+        te.us = best * 1e3;
+        tune_store(key, te);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return bail(cuda_fail(e, "batch tuning"));
+    std::vector<int> all(count);
+    for (int32_t i = 0; i < count; ++i)
+        all[i] = i;
+    std::vector<BatchItem> items;
+    make_items(*b, all, rpi, items);
+    gcoo_status s = upload_items(*b, items, st);
+    if (s != GCOO_SUCCESS)
+        return bail(s);
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return bail(cuda_fail(e, "batch queue upload"));
+
+    // capture [reset counter, (B -> BF16), persistent kernel] once
+    e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaMemsetAsync(b->counter.ptr, 0, sizeof(unsigned), b->cap);
+        if (prec == GCOO_PREC_BF16)
+            batch_bf16_kernel<<<dim3(64, static_cast<unsigned>(segs.size())), 256, 0, b->cap>>>(b->d_segs.ptr);
+        if (prec == GCOO_PREC_BF16)
+            batch_kernel<true><<<b->grid, kBatchThreads, 0, b->cap>>>(b->d_probs.ptr, b->d_items.ptr, b->nitems, b->counter.ptr);
+        else
+            batch_kernel<false><<<b->grid, kBatchThreads, 0, b->cap>>>(b->d_probs.ptr, b->d_items.ptr, b->nitems, b->counter.ptr);
+        e = cudaStreamEndCapture(b->cap, &b->graph);
+    }
+    if (e == cudaSuccess)
+        e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (e != cudaSuccess)
+        return bail(cuda_fail(e, "batch graph capture"));
+    *out = b;
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_batch_run(gcoo_batch *b, void *stream)
+{
+    if (!b || !b->exec)
+        return fail(GCOO_ERROR_INVALID_VALUE, "batch is NULL or not created");
+    GCOO_CUDA(cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream)));
+    count_launches(b->prec == GCOO_PREC_BF16 ? 2 : 1);
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_batch_launches(const gcoo_batch *b, int32_t *launches)
+{
+    if (!b || !launches)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL argument");
+    *launches = b->prec == GCOO_PREC_BF16 ? 2 : 1;
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_batch_destroy(gcoo_batch *b)
+{
+    delete b;
+    return GCOO_SUCCESS;
+}
+
+} // extern "C"

@@ -285,6 +285,130 @@ scatter_kernel(const float *__restrict__ A, int64_t m, int64_t k, const int32_t 
     }
 }
 
+// Vectorised scatter (k % 4 == 0, 16-byte aligned A): each thread owns 4
+// consecutive columns of the group's rows (one 128-bit load per row), so a
+// CTA covers 1024 columns per step. The per-row counts of a thread (0..4)
+// are packed four to a word in 8-bit fields and one warp scan of the packed
+// words gives, at once, every row's rank among the lanes (row order) and,
+// summed over the rows, the column-major rank (the reference's GCOO order).
+template <int CPG>
+__global__ void __launch_bounds__(kScatterThreads)
+scatter_vec_kernel(const float *__restrict__ A, int64_t m, int64_t k, const int32_t *__restrict__ group_index,
+                   const int32_t *__restrict__ row_ptr, float *__restrict__ vals, int32_t *__restrict__ rows,
+                   int32_t *__restrict__ cols, Entry *__restrict__ packed)
+{
+    constexpr int W = kScatterThreads / 32;
+    constexpr int NP = (CPG + 3) / 4;
+    constexpr int kTileCols = kScatterThreads * 4;
+    __shared__ uint32_t s_tot[W][NP];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t g = blockIdx.x;
+    const int64_t r0 = g * CPG;
+    const int nrows = static_cast<int>(r0 + CPG <= m ? CPG : m - r0);
+    const int64_t gbase = group_index ? group_index[g] : 0;
+    int32_t row_base[CPG];
+    int row_run[CPG];
+#pragma unroll
+    for (int r = 0; r < CPG; ++r) {
+        row_base[r] = (r < nrows && packed) ? row_ptr[r0 + r] : 0;
+        row_run[r] = 0;
+    }
+    int64_t col_run = 0;
+
+    for (int64_t c0 = 0; c0 < k; c0 += kTileCols) {
+        const int64_t c = c0 + threadIdx.x * 4;
+        float4 v[CPG];
+#pragma unroll
+        for (int r = 0; r < CPG; ++r)
+            v[r] = (r < nrows && c < k) ? __ldcs(reinterpret_cast<const float4 *>(A + (r0 + r) * k + c))
+                                        : make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t bits[CPG];
+        uint32_t word[NP];
+#pragma unroll
+        for (int i = 0; i < NP; ++i)
+            word[i] = 0;
+#pragma unroll
+        for (int r = 0; r < CPG; ++r) {
+            bits[r] = nz(v[r].x) | (nz(v[r].y) << 1) | (nz(v[r].z) << 2) | (nz(v[r].w) << 3);
+            word[r / 4] |= static_cast<uint32_t>(__popc(bits[r])) << (8 * (r % 4));
+        }
+        uint32_t incl[NP];
+#pragma unroll
+        for (int i = 0; i < NP; ++i) {
+            incl[i] = word[i];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl[i], d);
+                if (lane >= d)
+                    incl[i] += y; // fields never carry: a field's prefix is at most 4 * 32
+            }
+            if (lane == 31)
+                s_tot[warp][i] = incl[i];
+        }
+        __syncthreads();
+        int before[CPG], tile[CPG], lane_ex[CPG];
+#pragma unroll
+        for (int r = 0; r < CPG; ++r) {
+            before[r] = 0;
+            tile[r] = 0;
+            lane_ex[r] = static_cast<int>(((incl[r / 4] - word[r / 4]) >> (8 * (r % 4))) & 0xffu);
+        }
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+#pragma unroll
+            for (int r = 0; r < CPG; ++r) {
+                const int x = static_cast<int>((s_tot[w][r / 4] >> (8 * (r % 4))) & 0xffu);
+                before[r] += w < warp ? x : 0;
+                tile[r] += x;
+            }
+        }
+        int64_t pos = gbase + col_run;
+#pragma unroll
+        for (int r = 0; r < CPG; ++r)
+            pos += before[r] + lane_ex[r];
+        // reference GCOO order: column, then row
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+#pragma unroll
+            for (int r = 0; r < CPG; ++r) {
+                if ((bits[r] >> q) & 1u) {
+                    if (vals) {
+                        const float x = q == 0 ? v[r].x : q == 1 ? v[r].y : q == 2 ? v[r].z : v[r].w;
+                        vals[pos] = x;
+                        rows[pos] = static_cast<int32_t>(r0 + r);
+                        cols[pos] = static_cast<int32_t>(c + q);
+                    }
+                    ++pos;
+                }
+            }
+        }
+        // execution layout: row, then column
+        if (packed) {
+#pragma unroll
+            for (int r = 0; r < CPG; ++r) {
+                int64_t q_pos = static_cast<int64_t>(row_base[r]) + row_run[r] + before[r] + lane_ex[r];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if ((bits[r] >> q) & 1u) {
+                        Entry e;
+                        e.col = static_cast<int32_t>(c + q);
+                        e.val = q == 0 ? v[r].x : q == 1 ? v[r].y : q == 2 ? v[r].z : v[r].w;
+                        packed[q_pos++] = e;
+                    }
+                }
+            }
+        }
+        int64_t tile_all = 0;
+#pragma unroll
+        for (int r = 0; r < CPG; ++r) {
+            row_run[r] += tile[r];
+            tile_all += tile[r];
+        }
+        col_run += tile_all;
+        __syncthreads();
+    }
+}
+
 int sm_count()
 {
     static int sms = 0;
@@ -366,6 +490,19 @@ cudaError_t launch_scatter(const float *A, int64_t m, int64_t k, int32_t cpg, co
     if (ng <= 0)
         return cudaSuccess;
     const unsigned grid = static_cast<unsigned>(ng);
+    if (k % 4 == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0 && cpg <= 8) {
+        switch (cpg) {
+        case 1: scatter_vec_kernel<1><<<grid, kScatterThreads, 0, st>>>(A, m, k, group_index, row_ptr, vals, rows, cols, packed); break;
+        case 2: scatter_vec_kernel<2><<<grid, kScatterThreads, 0, st>>>(A, m, k, group_index, row_ptr, vals, rows, cols, packed); break;
+        case 4: scatter_vec_kernel<4><<<grid, kScatterThreads, 0, st>>>(A, m, k, group_index, row_ptr, vals, rows, cols, packed); break;
+        case 8: scatter_vec_kernel<8><<<grid, kScatterThreads, 0, st>>>(A, m, k, group_index, row_ptr, vals, rows, cols, packed); break;
+        case 16: scatter_vec_kernel<16><<<grid, kScatterThreads, 0, st>>>(A, m, k, group_index, row_ptr, vals, rows, cols, packed); break;
+        case 32: scatter_vec_kernel<32><<<grid, kScatterThreads, 0, st>>>(A, m, k, group_index, row_ptr, vals, rows, cols, packed); break;
+        default: return cudaErrorInvalidValue;
+        }
+        count_launches(1);
+        return cudaGetLastError();
+    }
     switch (cpg) {
     case 1: scatter_kernel<1><<<grid, kScatterThreads, 0, st>>>(A, m, k, group_index, row_ptr, vals, rows, cols, packed); break;
     case 2: scatter_kernel<2><<<grid, kScatterThreads, 0, st>>>(A, m, k, group_index, row_ptr, vals, rows, cols, packed); break;

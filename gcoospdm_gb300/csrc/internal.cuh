@@ -114,6 +114,15 @@ cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_
 cudaError_t launch_spdm_view(const gcoo_view &a, const float *B, int64_t n, float *C,
                              cudaStream_t st);
 
+// ---- autotune table (autotune.cu) ------------------------------------------------------
+struct TuneEntry {
+    int vec = 0, warps = 0, col_warps = 0, rows_per_item = 0;
+    double us = 0.0;
+};
+std::string bucket_key(int64_t m, int64_t k, int64_t nnz, int64_t n);
+bool tune_lookup(const std::string &key, TuneEntry *out);
+void tune_store(const std::string &key, const TuneEntry &e);
+
 // ---- FP64 check (errnorm.cu) -----------------------------------------------------------
 cudaError_t launch_error_norm(const Entry *packed, const int32_t *row_ptr, int64_t m,
                               const float *B, int64_t n, const float *C, double *acc2,
