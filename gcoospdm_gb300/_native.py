@@ -49,7 +49,8 @@ class GcooError(RuntimeError):
 
 class Params(C.Structure):
     _fields_ = [("rows_per_group", C.c_int32), ("vec", C.c_int32), ("warps", C.c_int32),
-                ("col_warps", C.c_int32), ("engine", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("col_warps", C.c_int32), ("engine", C.c_int32), ("depth", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
 
 
 class View(C.Structure):

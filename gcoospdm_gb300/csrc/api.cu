@@ -99,12 +99,12 @@ gcoo_status spdm_fp32(gcoo_handle *h, const float *dB, int64_t n, float *dC, cud
             p.vec = t.vec;
             p.warps = t.warps;
             p.col_warps = t.col_warps;
+            p.depth = t.depth;
         }
     }
-    const LaunchShape s = pick_shape(p, h->m, n, h->nnz, reinterpret_cast<uintptr_t>(dB),
+    const LaunchShape s = pick_shape(p, h->m, n, h->nnz, h->max_row_nnz, reinterpret_cast<uintptr_t>(dB),
                                      reinterpret_cast<uintptr_t>(dC));
-    cudaError_t e = launch_spdm_fp32(h->packed.ptr, h->row_ptr.ptr, h->m, h->p.rows_per_group, dB, n, dC, s,
-                                     h->status.ptr, st);
+    cudaError_t e = launch_spdm_fp32(h->packed.ptr, h->row_ptr.ptr, h->m, dB, n, dC, s, h->status.ptr, st);
     if (e != cudaSuccess)
         return cuda_fail(e, "spdm_fp32_kernel launch");
     return GCOO_SUCCESS;
@@ -180,6 +180,8 @@ gcoo_status gcoo_create(gcoo_handle **out, const float *dA, int64_t m, int64_t k
         return fail(GCOO_ERROR_INVALID_VALUE, "warps / col_warps out of range");
     if (p.engine < GCOO_ENGINE_AUTO || p.engine > GCOO_ENGINE_TENSOR)
         return fail(GCOO_ERROR_INVALID_VALUE, "unknown engine");
+    if (p.depth < 0 || p.depth > 2)
+        return fail(GCOO_ERROR_INVALID_VALUE, "depth must be 0, 1 or 2");
     gcoo_handle *h = new (std::nothrow) gcoo_handle();
     if (!h)
         return fail(GCOO_ERROR_ALLOC, "host allocation of the handle failed");
@@ -200,16 +202,20 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
     h->built = false;
     const size_t sc = scan_scratch_elems(h->m);
     if (!h->row_ptr.ensure(static_cast<size_t>(h->m) + 1) || !h->groups.ensure(2 * static_cast<size_t>(h->ng + 1)) ||
-        !h->scratch.ensure(sc + 1) || !h->status.ensure(1))
+        !h->scratch.ensure(sc + 2) || !h->status.ensure(1))
         return fail(GCOO_ERROR_ALLOC, "device allocation of the GCOO index arrays failed");
     GCOO_CUDA(cudaMemsetAsync(h->status.ptr, 0, sizeof(uint32_t), st));
+    int64_t *d_total = h->scratch.ptr + sc; // [0] total nnz, [1] longest row
+    GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, sizeof(int64_t), st));
     GCOO_CUDA(launch_row_count(h->dA, h->m, h->k, h->row_ptr.ptr, st));
-    int64_t *d_total = h->scratch.ptr + sc;
     GCOO_CUDA(launch_row_scan(h->row_ptr.ptr, h->m, h->p.rows_per_group, h->group_index(), h->nnz_per_group(),
                               d_total, h->scratch.ptr, h->status.ptr, st));
-    int64_t total = 0;
-    GCOO_CUDA(cudaMemcpyAsync(&total, d_total, sizeof(total), cudaMemcpyDeviceToHost, st));
+    GCOO_CUDA(launch_row_max(h->row_ptr.ptr, h->m, d_total + 1, st));
+    int64_t tot2[2] = {0, 0};
+    GCOO_CUDA(cudaMemcpyAsync(tot2, d_total, sizeof(tot2), cudaMemcpyDeviceToHost, st));
     GCOO_CUDA(cudaStreamSynchronize(st));
+    const int64_t total = tot2[0];
+    h->max_row_nnz = tot2[1];
     if (total < 0 || total > 0x7fffffffLL)
         return fail(GCOO_ERROR_FORMAT, "nnz = " + std::to_string(total) + " exceeds the int32 GCOO format");
     const size_t nnz = static_cast<size_t>(total);

@@ -65,6 +65,7 @@ bool tuned_params(int64_t m, int64_t k, int64_t nnz, int64_t n, gcoo_params *out
     out->vec = e.vec;
     out->warps = e.warps;
     out->col_warps = e.col_warps;
+    out->depth = e.depth;
     return true;
 }
 
@@ -93,20 +94,24 @@ gcoo_status gcoo_autotune(gcoo_handle *h, const float *dB, int64_t n, float *dC,
     std::vector<gcoo_params> cands;
     for (int vec : {1, 2, 4}) {
         for (int warps : {4, 8, 16, 32}) {
-            if (warps < cpg)
-                continue;
-            gcoo_params p = h->p;
-            p.vec = vec;
-            p.warps = warps;
-            p.col_warps = 0;
-            cands.push_back(p);
+            for (int depth : {1, 2}) {
+                if (warps < cpg)
+                    continue;
+                gcoo_params p = h->p;
+                p.vec = vec;
+                p.warps = warps;
+                p.col_warps = 0;
+                p.depth = depth;
+                cands.push_back(p);
+            }
         }
     }
     double best_us = 1e30;
     gcoo_params best_p = h->p;
     LaunchShape best_shape{};
     for (const gcoo_params &p : cands) {
-        const LaunchShape s = pick_shape(p, h->m, n, h->nnz, reinterpret_cast<uintptr_t>(dB), reinterpret_cast<uintptr_t>(dC));
+        const LaunchShape s = pick_shape(p, h->m, n, h->nnz, h->max_row_nnz, reinterpret_cast<uintptr_t>(dB),
+                                         reinterpret_cast<uintptr_t>(dC));
         if (s.vec != p.vec)
             continue; // not valid for this width / alignment
         gcoo_status r = spdm_fp32(h, dB, n, dC, st, &p); // warm-up
@@ -138,6 +143,7 @@ gcoo_status gcoo_autotune(gcoo_handle *h, const float *dB, int64_t n, float *dC,
     e.vec = best_shape.vec;
     e.warps = best_shape.warps;
     e.col_warps = best_shape.col_warps;
+    e.depth = best_shape.depth;
     e.us = best_us;
     tune_store(bucket_key(h->m, h->k, h->nnz, n), e);
     if (best) {
@@ -145,6 +151,7 @@ gcoo_status gcoo_autotune(gcoo_handle *h, const float *dB, int64_t n, float *dC,
         best->vec = e.vec;
         best->warps = e.warps;
         best->col_warps = e.col_warps;
+        best->depth = e.depth;
     }
     return GCOO_SUCCESS;
 }
@@ -161,8 +168,8 @@ gcoo_status gcoo_autotune_save(const char *path)
     size_t i = 0;
     for (const auto &kv : g_table) {
         const TuneEntry &e = kv.second;
-        fprintf(f, "{\"bucket\": \"%s\", \"vec\": %d, \"warps\": %d, \"col_warps\": %d, \"rows_per_item\": %d, \"us\": %.3f}%s\n",
-                kv.first.c_str(), e.vec, e.warps, e.col_warps, e.rows_per_item, e.us, ++i < g_table.size() ? "," : "");
+        fprintf(f, "{\"bucket\": \"%s\", \"vec\": %d, \"warps\": %d, \"col_warps\": %d, \"depth\": %d, \"rows_per_item\": %d, \"us\": %.3f}%s\n",
+                kv.first.c_str(), e.vec, e.warps, e.col_warps, e.depth, e.rows_per_item, e.us, ++i < g_table.size() ? "," : "");
     }
     fprintf(f, "]}\n");
     fclose(f);
@@ -181,8 +188,8 @@ gcoo_status gcoo_autotune_load(const char *path)
     while (fgets(line, sizeof line, f)) {
         char bucket[128];
         TuneEntry e;
-        if (sscanf(line, " {\"bucket\": \"%127[^\"]\", \"vec\": %d, \"warps\": %d, \"col_warps\": %d, \"rows_per_item\": %d, \"us\": %lf",
-                   bucket, &e.vec, &e.warps, &e.col_warps, &e.rows_per_item, &e.us) == 6) {
+        if (sscanf(line, " {\"bucket\": \"%127[^\"]\", \"vec\": %d, \"warps\": %d, \"col_warps\": %d, \"depth\": %d, \"rows_per_item\": %d, \"us\": %lf",
+                   bucket, &e.vec, &e.warps, &e.col_warps, &e.depth, &e.rows_per_item, &e.us) == 7) {
             tune_store(bucket, e);
             ++loaded;
         }

@@ -439,6 +439,36 @@ cudaError_t launch_row_count(const float *A, int64_t m, int64_t k, int32_t *row_
     return cudaGetLastError();
 }
 
+namespace {
+__global__ void row_max_kernel(const int32_t *__restrict__ row_ptr, int64_t m, unsigned long long *__restrict__ out)
+{
+    long long mx = 0;
+    for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < m;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const long long len = row_ptr[r + 1] - row_ptr[r];
+        mx = len > mx ? len : mx;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = y > mx ? y : mx;
+    }
+    if ((threadIdx.x & 31) == 0 && mx > 0)
+        atomicMax(out, static_cast<unsigned long long>(mx));
+}
+} // namespace
+
+cudaError_t launch_row_max(const int32_t *row_ptr, int64_t m, int64_t *out, cudaStream_t st)
+{
+    int64_t blocks = (m + 255) / 256;
+    if (blocks > 1024)
+        blocks = 1024;
+    row_max_kernel<<<static_cast<unsigned>(blocks < 1 ? 1 : blocks), 256, 0, st>>>(
+        row_ptr, m, reinterpret_cast<unsigned long long *>(out));
+    count_launches(1);
+    return cudaGetLastError();
+}
+
 size_t scan_scratch_elems(int64_t m)
 {
     const int64_t nb = (m + kScanTile - 1) / kScanTile;

@@ -17,6 +17,7 @@ struct gcoo_handle {
     int64_t ng = 0;
     bool built = false;
     int64_t nnz = 0;
+    int64_t max_row_nnz = 0;
 
     gcoo::DevBuf<int32_t> row_ptr;   // m + 1 (row counts, then exclusive prefix)
     gcoo::DevBuf<int32_t> groups;    // group_index[ng+1] | nnz_per_group[ng+1]

@@ -103,12 +103,16 @@ struct LaunchShape {
     int vec;       // columns per thread (1, 2, 4)
     int warps;     // warps per CTA
     int col_warps; // warps side by side on one row
+    int depth;     // 1: plain batches, 2: B loads of the next batch in flight
+    int rows;      // rows per CTA
 };
-LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz,
+LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, int64_t max_row,
                        uintptr_t b_addr, uintptr_t c_addr);
-cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_t m,
-                             int32_t rows_per_group, const float *B, int64_t n, float *C,
-                             const LaunchShape &s, uint32_t *status, cudaStream_t st);
+cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_t m, const float *B,
+                             int64_t n, float *C, const LaunchShape &s, uint32_t *status,
+                             cudaStream_t st);
+// Longest row (row_ptr[r+1] - row_ptr[r]) into *out (an int64 zeroed by the caller).
+cudaError_t launch_row_max(const int32_t *row_ptr, int64_t m, int64_t *out, cudaStream_t st);
 // Multiply straight from reference-layout GCOO arrays (column-major order
 // inside a group): one thread per column per group row.
 cudaError_t launch_spdm_view(const gcoo_view &a, const float *B, int64_t n, float *C,
@@ -116,7 +120,7 @@ cudaError_t launch_spdm_view(const gcoo_view &a, const float *B, int64_t n, floa
 
 // ---- autotune table (autotune.cu) ------------------------------------------------------
 struct TuneEntry {
-    int vec = 0, warps = 0, col_warps = 0, rows_per_item = 0;
+    int vec = 0, warps = 0, col_warps = 0, depth = 0, rows_per_item = 0;
     double us = 0.0;
 };
 std::string bucket_key(int64_t m, int64_t k, int64_t nnz, int64_t n);

@@ -56,11 +56,48 @@ struct Vec<1> {
     static __device__ __forceinline__ void store(float *p, const float (&o)[1]) { *p = o[0]; }
 };
 
-template <int V, int U>
+template <int V, int U, bool PIPE>
 __device__ __forceinline__ void row_chain(const Entry *__restrict__ s, int cnt, const float *__restrict__ Bj,
                                           int64_t n, float (&acc)[V])
 {
     int i = 0;
+    if (PIPE && cnt >= 2 * U) {
+        // software pipeline: the B loads of batch i+1 are in flight while
+        // batch i is accumulated (the fmaf order per element is unchanged)
+        float a[U], b[U][V], a2[U], b2[U][V];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const Entry e = s[u];
+            a[u] = e.val;
+            Vec<V>::load(Bj + static_cast<int64_t>(e.col) * n, b[u]);
+        }
+#pragma unroll 1
+        for (i = U; i + U <= cnt; i += U) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const Entry e = s[i + u];
+                a2[u] = e.val;
+                Vec<V>::load(Bj + static_cast<int64_t>(e.col) * n, b2[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    acc[v] = fmaf(a[u], b[u][v], acc[v]);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                a[u] = a2[u];
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    b[u][v] = b2[u][v];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                acc[v] = fmaf(a[u], b[u][v], acc[v]);
+    }
 #pragma unroll 1
     for (; i + U <= cnt; i += U) {
         Entry e[U];
@@ -90,7 +127,7 @@ __device__ __forceinline__ void row_chain(const Entry *__restrict__ s, int cnt, 
 
 // MAXT bounds the CTA size (rows_per_group * col_warps warps); the 1024-thread
 // variant (rows_per_group 32) unrolls less to stay within 64 registers.
-template <int V, int MAXT>
+template <int V, int MAXT, bool PIPE>
 __global__ void __launch_bounds__(MAXT)
 spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ row_ptr, int64_t m,
                  int32_t cpg, const float *__restrict__ B, int64_t n, float *__restrict__ C,
@@ -153,7 +190,7 @@ spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ r
         const int64_t lo = rs > cs ? rs : cs;
         const int64_t hi = re < ce ? re : ce;
         if (has_col && lo < hi)
-            row_chain<V, (MAXT > 512 ? 4 : 8)>(s_nz + (lo - a0), static_cast<int>(hi - lo), Bj, n, acc);
+            row_chain<V, (MAXT > 512 ? 4 : 8), PIPE>(s_nz + (lo - a0), static_cast<int>(hi - lo), Bj, n, acc);
         __syncthreads(); // buffer free before the next copy
     }
     if (has_row && has_col && ok)
@@ -195,12 +232,17 @@ spdm_view_kernel(const float *__restrict__ vals, const int32_t *__restrict__ row
 
 } // namespace
 
-LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, uintptr_t b_addr,
-                       uintptr_t c_addr)
+LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, int64_t max_row,
+                       uintptr_t b_addr, uintptr_t c_addr)
 {
-    (void)m;
-    (void)nnz;
     LaunchShape s;
+    // Heavy-tailed row lengths (the longest row far above the mean): one row
+    // per CTA, so a long row does not hold its group's other rows back, and
+    // the next batch's B loads in flight, since a long row is one long
+    // dependent chain. The per-element fmaf order is the same either way.
+    const double mean = m > 0 ? static_cast<double>(nnz) / static_cast<double>(m) : 0.0;
+    const bool skewed = max_row >= 256 && static_cast<double>(max_row) > 8.0 * (mean > 1.0 ? mean : 1.0);
+    s.rows = skewed ? 1 : p.rows_per_group;
     int vmax = 4;
     if (n % 4 != 0 || (b_addr & 15) || (c_addr & 15))
         vmax = 2;
@@ -212,7 +254,7 @@ LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, 
     if (v != 1 && v != 2 && v != 4)
         v = 1;
     s.vec = v;
-    const int cpg = p.rows_per_group;
+    const int cpg = s.rows;
     int cw;
     if (p.col_warps > 0)
         cw = p.col_warps;
@@ -229,13 +271,14 @@ LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, 
         cw = 32 / cpg > 0 ? 32 / cpg : 1;
     s.col_warps = cw;
     s.warps = cw * cpg;
+    s.depth = p.depth > 0 ? p.depth : (skewed ? 2 : 1);
     return s;
 }
 
-cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_t m, int32_t cpg,
-                             const float *B, int64_t n, float *C, const LaunchShape &s, uint32_t *status,
-                             cudaStream_t st)
+cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_t m, const float *B, int64_t n,
+                             float *C, const LaunchShape &s, uint32_t *status, cudaStream_t st)
 {
+    const int32_t cpg = s.rows; // rows per CTA (any value gives the same fmaf chains)
     const int64_t ng = (m + cpg - 1) / cpg;
     const int64_t tile = static_cast<int64_t>(s.col_warps) * 32 * s.vec;
     const int64_t ny = (n + tile - 1) / tile;
@@ -245,17 +288,23 @@ cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_
         return cudaErrorInvalidConfiguration;
     dim3 grid(static_cast<unsigned>(ng), static_cast<unsigned>(ny));
     const int threads = s.warps * 32;
-#define GCOO_FP32_LAUNCH(V, T)                                                                          \
-    spdm_fp32_kernel<V, T><<<grid, threads, kSmemBytes, st>>>(packed, row_ptr, m, cpg, B, n, C, s.col_warps, status)
+#define GCOO_FP32_LAUNCH(V, T, P)                                                                       \
+    spdm_fp32_kernel<V, T, P><<<grid, threads, kSmemBytes, st>>>(packed, row_ptr, m, cpg, B, n, C, s.col_warps, status)
+#define GCOO_FP32_VEC(T, P)                                                                             \
+    do {                                                                                                \
+        if (s.vec == 4) GCOO_FP32_LAUNCH(4, T, P);                                                      \
+        else if (s.vec == 2) GCOO_FP32_LAUNCH(2, T, P);                                                 \
+        else GCOO_FP32_LAUNCH(1, T, P);                                                                 \
+    } while (0)
+    const bool pipe = s.depth >= 2;
     if (threads <= 512) {
-        if (s.vec == 4) GCOO_FP32_LAUNCH(4, 512);
-        else if (s.vec == 2) GCOO_FP32_LAUNCH(2, 512);
-        else GCOO_FP32_LAUNCH(1, 512);
+        if (pipe) GCOO_FP32_VEC(512, true);
+        else GCOO_FP32_VEC(512, false);
     } else {
-        if (s.vec == 4) GCOO_FP32_LAUNCH(4, 1024);
-        else if (s.vec == 2) GCOO_FP32_LAUNCH(2, 1024);
-        else GCOO_FP32_LAUNCH(1, 1024);
+        if (pipe) GCOO_FP32_VEC(1024, true);
+        else GCOO_FP32_VEC(1024, false);
     }
+#undef GCOO_FP32_VEC
 #undef GCOO_FP32_LAUNCH
     count_launches(1);
     return cudaGetLastError();

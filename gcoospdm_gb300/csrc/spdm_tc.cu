@@ -217,7 +217,7 @@ spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_
     }
     if (warp == 2) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(N)
+                     "r"(N * (SPLIT ? 2 : 1))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -225,6 +225,10 @@ spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    // split-BF16 alternates two accumulator banks by tile parity (shorter
+    // FP32 accumulation chains in the tensor pipe); the epilogue adds them
+    constexpr int BANKS = SPLIT ? 2 : 1;
+    const int banks_used = ntiles >= BANKS ? BANKS : 1;
 
     if (ntiles > 0) {
         if (warp == 0 && lane == 0) {
@@ -264,12 +268,15 @@ spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_
                 const uint32_t st = smem_u32(stages + static_cast<size_t>(s) * Cfg::kStage);
                 const uint64_t ah = smem_desc_sw32(st);
                 const uint64_t bh = smem_desc_sw32(st + Cfg::kABytes);
-                tc_mma(tmem, ah, bh, idesc, i > 0 ? 1u : 0u);
+                const uint32_t d = tmem + static_cast<uint32_t>((i % BANKS) * N);
+                tc_mma(d, ah, bh, idesc, i >= BANKS ? 1u : 0u);
                 if (SPLIT) {
+                    // (ah + al)(bh + bl): all four products
                     const uint64_t al = smem_desc_sw32(st + kTileBytes);
                     const uint64_t bl = smem_desc_sw32(st + Cfg::kABytes + N * 32);
-                    tc_mma(tmem, ah, bl, idesc, 1u);
-                    tc_mma(tmem, al, bh, idesc, 1u);
+                    tc_mma(d, ah, bl, idesc, 1u);
+                    tc_mma(d, al, bh, idesc, 1u);
+                    tc_mma(d, al, bl, idesc, 1u);
                 }
                 tc_commit(&empty[s]); // slot reusable once these MMAs have read it
             }
@@ -287,6 +294,13 @@ spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_
             for (int c = 0; c < N; c += 32) {
                 float v[32];
                 tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c), v);
+                if (BANKS == 2 && banks_used == 2) {
+                    float w[32];
+                    tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(N + c), w);
+#pragma unroll
+                    for (int q = 0; q < 32; ++q)
+                        v[q] += w[q];
+                }
                 const int64_t j = jt * N + c;
                 if (row < m && j < n) {
                     float *out = C + row * n + j;
@@ -319,11 +333,15 @@ spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_
     __syncthreads();
     if (warp == 2) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(N) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(N * (SPLIT ? 2 : 1))
+                     : "memory");
     }
 }
 
-int tile_n_for(int64_t n) { return n >= 256 ? 256 : 128; }
+// Output columns per CTA. A CTA's ring is sized (~98 KB) so that two CTAs
+// share an SM; split-BF16 keeps two accumulator banks, so it uses 128-column
+// tiles to stay within half of the 512 tensor-memory columns.
+int tile_n_for(int64_t n, bool split) { return (!split && n >= 256) ? 256 : 128; }
 
 template <int N, int S, bool SPLIT>
 cudaError_t launch_tc(const TcPlan &p, int64_t m, int64_t n, float *C, uint32_t *status, cudaStream_t st)
@@ -400,7 +418,7 @@ double tc_density(const gcoo_handle *h)
 gcoo_status tc_prepare_b(gcoo_handle *h, int64_t n)
 {
     TcPlan &p = *h->tc;
-    const int N = tile_n_for(n);
+    const int N = tile_n_for(n, p.split);
     const int64_t nt = (n + N - 1) / N;
     const size_t elems = static_cast<size_t>(nt) * p.kb * N * kTileK;
     if (!p.b_hi.ensure(elems) || (p.split && !p.b_lo.ensure(elems)))
@@ -412,7 +430,7 @@ gcoo_status tc_prepare_b(gcoo_handle *h, int64_t n)
 gcoo_status tc_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, cudaStream_t st)
 {
     TcPlan &p = *h->tc;
-    const int N = tile_n_for(n);
+    const int N = tile_n_for(n, p.split);
     dim3 g(static_cast<unsigned>(p.kb), static_cast<unsigned>((n + N - 1) / N));
     b_tiles_kernel<<<g, 256, 0, st>>>(dB, h->k, n, N, p.kb, reinterpret_cast<__nv_bfloat16 *>(p.b_hi.ptr),
                                       p.split ? reinterpret_cast<__nv_bfloat16 *>(p.b_lo.ptr) : nullptr);
@@ -420,11 +438,11 @@ gcoo_status tc_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, cudaS
     GCOO_LAUNCH("b_tiles_kernel");
     cudaError_t e;
     if (N == 256)
-        e = p.split ? launch_tc<256, 6, true>(p, h->m, n, dC, h->status.ptr, st)
-                    : launch_tc<256, 8, false>(p, h->m, n, dC, h->status.ptr, st);
+        e = launch_tc<256, 8, false>(p, h->m, n, dC, h->status.ptr, st);
+    else if (N == 128 && !p.split)
+        e = launch_tc<128, 12, false>(p, h->m, n, dC, h->status.ptr, st);
     else
-        e = p.split ? launch_tc<128, 8, true>(p, h->m, n, dC, h->status.ptr, st)
-                    : launch_tc<128, 12, false>(p, h->m, n, dC, h->status.ptr, st);
+        e = launch_tc<128, 6, true>(p, h->m, n, dC, h->status.ptr, st);
     if (e != cudaSuccess)
         return cuda_fail(e, "spdm_tc_kernel launch");
     return GCOO_SUCCESS;

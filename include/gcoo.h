@@ -73,7 +73,8 @@ typedef struct gcoo_params {
     int32_t warps;          /* warps per CTA: 0 auto, 1..32                 */
     int32_t col_warps;      /* warps side by side on one row: 0 auto        */
     int32_t engine;         /* gcoo_engine for non-FP32 forms               */
-    int32_t reserved[3];
+    int32_t depth;          /* B-load pipelining: 0 auto, 1 off, 2 on        */
+    int32_t reserved[2];
 } gcoo_params;
 
 typedef struct gcoo_handle gcoo_handle;
