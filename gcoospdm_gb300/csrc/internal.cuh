@@ -174,9 +174,13 @@ __device__ __forceinline__ uint64_t global_ns()
     return t;
 }
 
+__device__ __forceinline__ bool mbar_wait_ns(uint64_t *bar, uint32_t parity, uint64_t limit_ns);
+
 // Returns true once the phase with the given parity has completed, false if
 // it has not completed within kWaitNs nanoseconds (or kWaitLimit polls).
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) { return mbar_wait_ns(bar, parity, kWaitNs); }
+
+__device__ __forceinline__ bool mbar_wait_ns(uint64_t *bar, uint32_t parity, uint64_t limit_ns)
 {
     const uint32_t addr = smem_u32(bar);
     uint64_t t0 = 0;
@@ -193,7 +197,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
         const uint64_t now = global_ns();
         if (it == 0)
             t0 = now;
-        else if (now - t0 > kWaitNs)
+        else if (now - t0 > limit_ns)
             return false;
     }
     return false;

@@ -151,6 +151,12 @@ gcoo_status gcoo_destroy(gcoo_handle *h);
  * the tcgen05 block path is taken. Builds nothing. */
 gcoo_status gcoo_query_engine(gcoo_handle *h, gcoo_precision prec, int32_t *tensor);
 
+/* No counterpart in the reference (it has no bounded waits). Runs the
+ * library's bounded mbarrier wait on a barrier nothing arrives on, with a
+ * limit of limit_ns (<= 2e9): returns GCOO_ERROR_TIMEOUT when the wait gave
+ * up and reported it, as it must; the context stays usable. */
+gcoo_status gcoo_check_bounded_wait(uint64_t limit_ns, void *stream);
+
 /* Number of kernels this library has launched in this process (all
  * handles, all entry points); lets a caller count launches in a region. */
 uint64_t gcoo_kernel_launches(void);
