@@ -40,7 +40,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=8192, help="m = k = n of the square workload")
+    ap.add_argument("--size", type=int, default=8192, help="m = k = n of the square workload")
     ap.add_argument("--sparsity", type=float, default=0.99)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -69,7 +69,7 @@ def run_case(args):
         res = run_batched(g, dg, torch, dev, count=64)
         print(json.dumps(res))
     else:
-        n = args.n
+        n = args.size
         A = dg.bernoulli_dense_torch(SEED, n, n, 1.0 - args.sparsity, device=dev)
         B = dg.dense_pm1_torch(SEED, 5, n, n, device=dev)
         h = g.GcooHandle(A).build()
@@ -203,7 +203,7 @@ def run_reference(args, rank, world):
     from gcoospdm_gb300 import datagen as dg
     import oracle
     oracle.build()
-    n = args.n
+    n = args.size
     p = 1.0 - args.sparsity
     B = dg.dense_pm1(SEED, 5, n, n)
     probe = dg.bernoulli_dense(SEED, 256, n, p)
@@ -252,7 +252,7 @@ def run_ours(args, rank, world, local, pg):
         g.build()
     torch.cuda.set_device(local)
     L = g.lib()
-    n = args.n
+    n = args.size
     m = k = n
     p = 1.0 - args.sparsity
     dev = torch.device("cuda", local)

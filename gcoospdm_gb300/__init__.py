@@ -86,6 +86,25 @@ class GcooHandle:
         check(lib().gcoo_create(C.byref(self._h), C.c_void_p(A.data_ptr()), self.m, self.k, C.byref(p)))
         self.rows_per_group = rows_per_group
 
+    @classmethod
+    def from_coo(cls, rows, cols, vals, m: int, k: int, rows_per_group: int = 4, **params) -> "GcooHandle":
+        """Handle built from device COO triplets (int32 rows/cols, float32 vals),
+        without a dense m x k buffer; duplicates: the later triplet wins."""
+        torch = _torch()
+        for t, dt in ((rows, torch.int32), (cols, torch.int32), (vals, torch.float32)):
+            if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != dt or not t.is_contiguous():
+                raise ValueError("rows/cols must be int32 and vals float32 contiguous CUDA tensors")
+        self = cls.__new__(cls)
+        self._A = (rows, cols, vals)  # the handle reads the triplets at build time
+        self.m, self.k = int(m), int(k)
+        self._h = C.c_void_p()
+        p = make_params(rows_per_group, **params)
+        check(lib().gcoo_create_coo(C.byref(self._h), self.m, self.k, C.c_void_p(rows.data_ptr()),
+                                    C.c_void_p(cols.data_ptr()), C.c_void_p(vals.data_ptr()), int(vals.numel()),
+                                    C.byref(p)))
+        self.rows_per_group = rows_per_group
+        return self
+
     @property
     def ptr(self):
         return self._h
@@ -141,6 +160,20 @@ class GcooHandle:
         else:
             check(lib().gcoo_spdm_ex(self._h, C.c_void_p(B.data_ptr()), n, C.c_void_p(Cout.data_ptr()),
                                      PREC[prec], s))
+        return Cout
+
+    def spdm_left(self, D, Cout=None, stream=None):
+        """C = D @ A (the other orientation): D is p x m, C is p x k."""
+        torch = _torch()
+        _check_f32(D, "D")
+        if D.dim() != 2 or D.shape[1] != self.m:
+            raise ValueError(f"D must be p x {self.m}")
+        p = int(D.shape[0])
+        if Cout is None:
+            Cout = torch.empty((p, self.k), dtype=torch.float32, device=D.device)
+        _check_f32(Cout, "C", (p, self.k))
+        check(lib().gcoo_spdm_left(self._h, C.c_void_p(D.data_ptr()), p, C.c_void_p(Cout.data_ptr()),
+                                   _stream_ptr(stream)))
         return Cout
 
     def prepare(self, n: int, prec: str, stream=None):
@@ -318,8 +351,16 @@ class ShGCOOSpDM(ShGemm):
         return 0.0
 
     def mutiply(self, B, nRows, nCols, C_):  # noqa: N802
-        # the reference's GCOO plugin leaves this empty (src/ShGCOOSpDM.h:21)
-        raise GcooError(5, "mutiply is not provided by the GCOO plugin")
+        """C = B x self (B nRows x nCols with nCols == self's rows); empty in the
+        reference's GCOO plugin (src/ShGCOOSpDM.h:21)."""
+        if tuple(B.shape) != (nRows, nCols) or nCols != self.m_nRows:
+            raise ValueError("B must be nRows x (rows of the sparse operand)")
+        if self._arrays is None:
+            self.build()
+            self._arrays = True
+        self._h.spdm_left(B, C_)
+        self._sync()
+        return 0.0
 
     def build(self):
         self._h.build()

@@ -28,8 +28,8 @@ ENGINE = {"auto": 0, "cuda_core": 1, "tensor": 2}
 # Every symbol include/gcoo.h declares (checked by the CPU test suite).
 EXPORTS = (
     "gcoo_abi_version", "gcoo_status_string", "gcoo_last_error", "gcoo_params_default",
-    "gcoo_set_allocator", "gcoo_create", "gcoo_build", "gcoo_export", "gcoo_spdm", "gcoo_spdm_ex",
-    "gcoo_prepare", "gcoo_multiply_by", "gcoo_destroy", "gcoo_query_engine", "gcoo_kernel_launches",
+    "gcoo_set_allocator", "gcoo_create", "gcoo_create_coo", "gcoo_build", "gcoo_export", "gcoo_spdm", "gcoo_spdm_ex",
+    "gcoo_prepare", "gcoo_multiply_by", "gcoo_destroy", "gcoo_spdm_left", "gcoo_query_engine", "gcoo_kernel_launches",
     "gcoo_check_bounded_wait",
     "gcoo_device_status",
     "gcoo_convert_count", "gcoo_convert_count_static", "gcoo_convert_scatter", "gcoo_spdm_view", "gcoo_error_norm",
@@ -89,6 +89,7 @@ def _declare(L) -> None:
         "gcoo_params_default": (st, [C.POINTER(Params)]),
         "gcoo_set_allocator": (st, [ALLOC_FN, FREE_FN, vp]),
         "gcoo_create": (st, [C.POINTER(vp), vp, i64, i64, C.POINTER(Params)]),
+        "gcoo_create_coo": (st, [C.POINTER(vp), i64, i64, vp, vp, vp, i64, C.POINTER(Params)]),
         "gcoo_build": (st, [vp, vp]),
         "gcoo_export": (st, [vp, C.POINTER(View)]),
         "gcoo_spdm": (st, [vp, vp, i64, vp, vp]),
@@ -96,6 +97,7 @@ def _declare(L) -> None:
         "gcoo_prepare": (st, [vp, i64, C.c_int, vp]),
         "gcoo_multiply_by": (st, [vp, vp, i64, vp, vp]),
         "gcoo_destroy": (st, [vp]),
+        "gcoo_spdm_left": (st, [vp, vp, i64, vp, vp]),
         "gcoo_query_engine": (st, [vp, C.c_int, C.POINTER(i32)]),
         "gcoo_kernel_launches": (C.c_uint64, []),
         "gcoo_check_bounded_wait": (st, [C.c_uint64, vp]),

@@ -62,6 +62,12 @@ void dev_free(void *p)
         cudaFree(p);
 }
 
+// coo.cu
+gcoo_status coo_build(gcoo_handle *h, cudaStream_t st);
+// left.cu
+gcoo_status left_prepare(gcoo_handle *h, LeftPlan *&plan, int64_t p, cudaStream_t st);
+gcoo_status left_spdm(gcoo_handle *h, const LeftPlan &L, const float *dD, int64_t p, float *dC, cudaStream_t st);
+
 // Implemented in forms.cu / autotune.cpp.
 gcoo_status run_form(gcoo_handle *h, const float *dB, int64_t n, float *dC, gcoo_precision prec,
                      cudaStream_t st, bool prepare_only);
@@ -200,6 +206,17 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
         return fail(GCOO_ERROR_INVALID_VALUE, "handle is NULL");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     h->built = false;
+    if (h->coo) {
+        gcoo_status s = coo_build(h, st);
+        if (s != GCOO_SUCCESS)
+            return s;
+        h->built = true;
+        destroy_tc_plan(h->tc);
+        h->tc = nullptr;
+        destroy_left_plan(h->left);
+        h->left = nullptr;
+        return GCOO_SUCCESS;
+    }
     const size_t sc = scan_scratch_elems(h->m);
     if (!h->row_ptr.ensure(static_cast<size_t>(h->m) + 1) || !h->groups.ensure(2 * static_cast<size_t>(h->ng + 1)) ||
         !h->scratch.ensure(sc + 2) || !h->status.ensure(1))
@@ -231,6 +248,49 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
     if (h->tc)
         destroy_tc_plan(h->tc);
     h->tc = nullptr;
+    destroy_left_plan(h->left);
+    h->left = nullptr;
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_spdm_left(gcoo_handle *h, const float *dD, int64_t p, float *dC, void *stream)
+{
+    if (!h || !dD || !dC)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL handle or matrix pointer");
+    if (!h->built)
+        return fail(GCOO_ERROR_NOT_BUILT, "gcoo_build has not run");
+    gcoo_status s = check_n(p);
+    if (s != GCOO_SUCCESS)
+        return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    s = left_prepare(h, h->left, p, st);
+    if (s != GCOO_SUCCESS)
+        return s;
+    return left_spdm(h, *h->left, dD, p, dC, st);
+}
+
+gcoo_status gcoo_create_coo(gcoo_handle **out, int64_t m, int64_t k, const int32_t *d_rows, const int32_t *d_cols,
+                            const float *d_vals, int64_t nnz, const gcoo_params *params)
+{
+    if (!out)
+        return fail(GCOO_ERROR_INVALID_VALUE, "out is NULL");
+    *out = nullptr;
+    if (nnz < 0 || (nnz > 0 && (!d_rows || !d_cols || !d_vals)))
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL triplet arrays or negative nnz");
+    if (nnz > 0x7fffffffLL)
+        return fail(GCOO_ERROR_FORMAT, "more triplets than the int32 GCOO format holds");
+    // reuse the dense constructor's validation with a placeholder operand
+    static const float placeholder = 0.0f;
+    gcoo_status s = gcoo_create(out, &placeholder, m, k, params);
+    if (s != GCOO_SUCCESS)
+        return s;
+    gcoo_handle *h = *out;
+    h->dA = nullptr;
+    h->coo = true;
+    h->coo_rows = d_rows;
+    h->coo_cols = d_cols;
+    h->coo_vals = d_vals;
+    h->coo_nnz = nnz;
     return GCOO_SUCCESS;
 }
 

@@ -6,12 +6,19 @@
 namespace gcoo {
 struct TcPlan;    // tensor-core tiles (spdm_tc.cu)
 struct LowpWork;  // low-precision workspaces (spdm_lowp.cu)
+struct LeftPlan;  // column-order layout for C = D x A (left.cu)
 void destroy_tc_plan(TcPlan *p);
 void destroy_lowp_work(LowpWork *w);
+void destroy_left_plan(LeftPlan *p);
 } // namespace gcoo
 
 struct gcoo_handle {
     const float *dA = nullptr;
+    // COO source (gcoo_create_coo): device triplets, not owned
+    bool coo = false;
+    const int32_t *coo_rows = nullptr, *coo_cols = nullptr;
+    const float *coo_vals = nullptr;
+    int64_t coo_nnz = 0;
     int64_t m = 0, k = 0;
     gcoo_params p{};
     int64_t ng = 0;
@@ -30,6 +37,7 @@ struct gcoo_handle {
 
     gcoo::TcPlan *tc = nullptr;
     gcoo::LowpWork *lowp = nullptr;
+    gcoo::LeftPlan *left = nullptr;
 
     int32_t *group_index() { return groups.ptr; }
     int32_t *nnz_per_group() { return groups.ptr + (ng + 1); }
@@ -38,5 +46,6 @@ struct gcoo_handle {
     {
         gcoo::destroy_tc_plan(tc);
         gcoo::destroy_lowp_work(lowp);
+        gcoo::destroy_left_plan(left);
     }
 };

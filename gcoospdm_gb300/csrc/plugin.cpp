@@ -64,14 +64,24 @@ double ShGCOOSpDM::mutiplyBy(float *A, int nRows, int nCols, float *C)
     return finish(s);
 }
 
+// C = B x self: B is nRows x nCols (nCols == the sparse operand's rows), C is
+// nRows x the sparse operand's columns. The reference leaves this empty.
 double ShGCOOSpDM::mutiply(float *B, int nRows, int nCols, float *C)
 {
-    (void)B;
-    (void)nRows;
-    (void)nCols;
-    (void)C;
-    m_status = GCOO_ERROR_UNSUPPORTED;
-    return -static_cast<double>(GCOO_ERROR_UNSUPPORTED);
+    if (!m_handle)
+        return finish(m_status != GCOO_SUCCESS ? m_status : GCOO_ERROR_INVALID_VALUE);
+    if (nCols != m_nRows)
+        return finish(GCOO_ERROR_INVALID_VALUE);
+    gcoo_status s = GCOO_SUCCESS;
+    gcoo_view v;
+    if (gcoo_export(m_handle, &v) != GCOO_SUCCESS) { // not built yet: convert first
+        s = gcoo_build(m_handle, m_stream);
+        if (s == GCOO_SUCCESS)
+            refreshView();
+    }
+    if (s == GCOO_SUCCESS)
+        s = gcoo_spdm_left(m_handle, B, nRows, C, m_stream);
+    return finish(s);
 }
 
 void ShGCOOSpDM::build()

@@ -25,7 +25,7 @@ class ShGCOOSpDM : public ShGemm
 
     // convert + multiply (src/ShGCOOSpDM.cu:131-180); A is k x n, C is m x n
     double mutiplyBy(float *A, int nRows, int nCols, float *C);
-    // the reference's empty stub (src/ShGCOOSpDM.h:21); reports UNSUPPORTED
+    // the other orientation, C = B x self (empty in the reference, src/ShGCOOSpDM.h:21)
     double mutiply(float *B, int nRows, int nCols, float *C);
     // conversion into members (src/ShGCOOSpDM.cu:182-193)
     void build();

@@ -115,6 +115,19 @@ gcoo_status gcoo_set_allocator(gcoo_alloc_fn alloc, gcoo_free_fn release, void *
 gcoo_status gcoo_create(gcoo_handle **out, const float *dA, int64_t m, int64_t k,
                         const gcoo_params *params);
 
+/* Sparse-input ingestion. The reference reaches GCOO only through a dense
+ * buffer (its Matrix Market reader densifies in file order,
+ * src/MatrixReader.cpp:11-84); this handle instead takes nnz COO triplets on
+ * the device (0-based, any order, not owned: they must stay valid while the
+ * handle builds from them). gcoo_build then yields exactly the arrays that
+ * writing the triplets into a zero m x k buffer in order (a later duplicate
+ * overwrites an earlier one) and converting it would give, without that
+ * buffer. An out-of-range index makes gcoo_build fail with
+ * GCOO_ERROR_INVALID_VALUE. */
+gcoo_status gcoo_create_coo(gcoo_handle **out, int64_t m, int64_t k, const int32_t *d_rows,
+                            const int32_t *d_cols, const float *d_vals, int64_t nnz,
+                            const gcoo_params *params);
+
 /* build() (src/ShGCOOSpDM.cu:182-193): dense -> GCOO conversion into
  * handle-owned arrays (count, device exclusive scan, stable scatter). Reads
  * the total nnz back to size the arrays, so it synchronises `stream` once.
@@ -146,6 +159,14 @@ gcoo_status gcoo_prepare(gcoo_handle *h, int64_t n, gcoo_precision prec, void *s
 gcoo_status gcoo_multiply_by(gcoo_handle *h, const float *dB, int64_t n, float *dC, void *stream);
 
 gcoo_status gcoo_destroy(gcoo_handle *h);
+
+/* mutiply() (src/ShGemm.h:16; the reference's GCOO plugin leaves it empty,
+ * src/ShGCOOSpDM.h:21): the other orientation, C = D x A with D dense p x m
+ * and C p x k (row-major), FP32, each C element a sequential fmaf chain over
+ * A's rows in ascending order. The first call (or a larger p) builds A's
+ * column-order layout and sizes the transposed operands: allocation and one
+ * synchronisation then, none on later calls of the same width. */
+gcoo_status gcoo_spdm_left(gcoo_handle *h, const float *dD, int64_t p, float *dC, void *stream);
 
 /* Form the handle would use for `prec` at width n: writes 1 to *tensor when
  * the tcgen05 block path is taken. Builds nothing. */

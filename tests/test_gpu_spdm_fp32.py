@@ -138,8 +138,25 @@ def test_plugin_mirror_and_builder(native, torch, manifest):
     assert g.runKernelTest(dB, 800, 800, C2) == 0.0
     assert torch.equal(C1, C2)
     assert native.SpGemmBuilder.getShGemmAlgo(dA, 800, 800, "csr") is None
-    with pytest.raises(native.GcooError):
-        g.mutiply(dB, 800, 800, C2)
+    # the other orientation: C = B x self
+    assert g.mutiply(dB, 800, 800, C2) == 0.0
+    ref = (dB.double() @ dA.double()).float()
+    assert float((C2 - ref).abs().max()) < 1e-4
+
+
+@pytest.mark.parametrize("m,k,p,s", [(300, 200, 96, 0.9), (1000, 777, 130, 0.98), (64, 4096, 512, 0.99)])
+def test_left_orientation_bit_identical(native, oracle_mod, torch, m, k, p, s):
+    """C = D x A equals, bit for bit, the oracle's chain on the transposed
+    problem (C^T = A^T x D^T: each C element over A's rows in order)."""
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense(80 + m, m, k, 1.0 - s)
+    D = dg.dense_pm1(80 + m, 5, p, m)
+    ref_t = oracle_mod.spdm(oracle_mod.convert(np.ascontiguousarray(A.T)), np.ascontiguousarray(D.T))
+    h = native.GcooHandle(dev(torch, A)).build()
+    Cg = h.spdm_left(dev(torch, D)).cpu().numpy()
+    assert same_bits(Cg, np.ascontiguousarray(ref_t.T))
+    Cg2 = h.spdm_left(dev(torch, D)).cpu().numpy()  # second call reuses the column layout
+    assert same_bits(Cg2, Cg)
 
 
 def test_multiply_by_steady_state_and_determinism(native, torch):
@@ -187,3 +204,23 @@ def test_full_size_fp32_within_tolerance(native, torch):
     from oracle import convert, spdm
     ref = spdm(convert(sub), B)
     assert np.array_equal(Cg[rows].cpu().numpy().view(np.uint32), ref.view(np.uint32))
+
+
+def test_fp32_multiply_replays_from_a_cuda_graph(native, torch):
+    """The persistent-handle path: build once, capture the multiply, replay it
+    with new B contents (no allocation or synchronisation inside gcoo_spdm)."""
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense_torch(29, 1024, 768, 0.02, device="cuda")
+    h = native.GcooHandle(A).build()
+    B = dg.dense_pm1_torch(29, 5, 768, 512, device="cuda")
+    Cd = torch.empty(1024, 512, device="cuda")
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s):
+        h.spdm(B, Cd, stream=s)
+    for seed in (30, 31):
+        B.copy_(dg.dense_pm1_torch(seed, 5, 768, 512, device="cuda"))
+        graph.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(Cd, h.spdm(B))
