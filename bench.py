@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the extra precision/batched lines")
+    ap.add_argument("--no-gpu-baselines", action="store_true",
+                    help="skip timing the reference algorithm, cuSPARSE and cuBLAS on the same GPU")
     ap.add_argument("--sweep", action="store_true", help="print the FP32 n x sparsity sweep instead")
     ap.add_argument("--case", choices=["tc_bf16", "tc_split", "convert", "fp32", "batched", "fp8", "bf16_fma"],
                     help="run one small case a few times (for profiling) and exit")
@@ -362,6 +364,10 @@ def run_ours(args, rank, world, local, pg):
     if not args.no_forms:
         forms = run_forms(args, g, dg, torch, dev)
 
+    gpu_baselines = None
+    if rank == 0 and world == 1 and not args.no_gpu_baselines:
+        gpu_baselines = run_gpu_baselines(g, torch, A, B, flop)
+
     if rank != 0:
         return
     line = {
@@ -387,6 +393,8 @@ def run_ours(args, rank, world, local, pg):
         "e2e": e2e,
         "cpu_baseline": cpu,
     }
+    if gpu_baselines:
+        line["gpu_baselines"] = gpu_baselines
     if forms:
         line["forms"] = forms
     print(json.dumps(line), flush=True)
@@ -499,6 +507,39 @@ def run_irregular(g, dg, torch, dev, m=65536, n=256, nnz=1_200_000):
     del A
     torch.cuda.empty_cache()
     return res
+
+
+def run_gpu_baselines(g, torch, A, B, flop):
+    """Same workload through the baselines built for this GPU: the reference's
+    GCOO algorithm restated on the GPU, cuSPARSE SpMM (CSR) and cuBLAS SGEMM on
+    the dense-with-zeros operand. Each: convert+multiply and multiply only."""
+    m, k = A.shape
+    n = B.shape[1]
+    Cd = torch.empty(m, n, device=A.device)
+    out = {}
+    try:
+        ref = g.RefAlgoBaseline(A)
+        e2e = _time(torch, lambda: ref.multiply_by(B, Cd), reps=3, warm=1)
+        ref.build()
+        ker = _time(torch, lambda: ref.run_kernel(B, Cd), reps=3, warm=1)
+        out["reference_algorithm_gcoo"] = {"multiply_by_ms": round(e2e, 4), "multiply_ms": round(ker, 4),
+                                           "multiply_gflops": round(flop / ker / 1e6, 1),
+                                           "note": "the reference's GCOO algorithm restated for the GPU"}
+        ref.close()
+    except Exception as e:
+        out["reference_algorithm_gcoo"] = {"error": f"{type(e).__name__}: {e}"}
+    for algo in ("cusparse", "cublas"):
+        try:
+            b = g.SpGemmBuilder.getShGemmAlgo(A, m, k, algo)
+            e2e = _time(torch, lambda: b.mutiplyBy(B, k, n, Cd), reps=3, warm=1)
+            b.build()
+            ker = _time(torch, lambda: b.runKernelTest(B, k, n, Cd), reps=3, warm=1)
+            out[algo] = {"multiply_by_ms": round(e2e, 4), "multiply_ms": round(ker, 4),
+                         "multiply_gflops": round(flop / ker / 1e6, 1)}
+            del b
+        except Exception as e:
+            out[algo] = {"error": f"{type(e).__name__}: {e}"}
+    return out
 
 
 def run_forms(args, g, dg, torch, dev):

@@ -399,6 +399,14 @@ class _BaselineGemm(ShGemm):
                 getattr(L, f).argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
             L.gcoo_baseline_build.argtypes = [C.c_void_p]
             L.gcoo_baseline_destroy.argtypes = [C.c_void_p]
+            L.gcoo_refalgo_create.restype = C.c_void_p
+            L.gcoo_refalgo_create.argtypes = [C.c_void_p, C.c_int64, C.c_int64]
+            for f in ("gcoo_refalgo_multiply_by", "gcoo_refalgo_run_kernel"):
+                getattr(L, f).restype = C.c_int
+                getattr(L, f).argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+            L.gcoo_refalgo_build.restype = C.c_int
+            L.gcoo_refalgo_build.argtypes = [C.c_void_p]
+            L.gcoo_refalgo_destroy.argtypes = [C.c_void_p]
             cls._L = L
         return cls._L
 
@@ -423,6 +431,44 @@ class _BaselineGemm(ShGemm):
         try:
             if self._g:
                 self._lib().gcoo_baseline_destroy(self._g)
+        except Exception:
+            pass
+
+
+class RefAlgoBaseline:
+    """Baseline only: the reference's GCOO algorithm restated for the GPU
+    (libgcoo_baselines.so): per-call allocation, single-thread serial scan,
+    one CTA per 4-row group, scalar B loads. Timed beside this library."""
+
+    def __init__(self, A):
+        _check_f32(A, "A")
+        self._A = A
+        self.m, self.k = int(A.shape[0]), int(A.shape[1])
+        self._L = _BaselineGemm._lib()
+        self._h = self._L.gcoo_refalgo_create(A.data_ptr(), self.m, self.k)
+
+    def multiply_by(self, B, Cout):
+        if self._L.gcoo_refalgo_multiply_by(self._h, B.data_ptr(), int(B.shape[1]), Cout.data_ptr()) != 0:
+            raise GcooError(3, "reference-algorithm baseline failed")
+        return Cout
+
+    def build(self):
+        if self._L.gcoo_refalgo_build(self._h) != 0:
+            raise GcooError(3, "reference-algorithm baseline build failed")
+
+    def run_kernel(self, B, Cout):
+        if self._L.gcoo_refalgo_run_kernel(self._h, B.data_ptr(), int(B.shape[1]), Cout.data_ptr()) != 0:
+            raise GcooError(3, "reference-algorithm baseline multiply failed")
+        return Cout
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.gcoo_refalgo_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 

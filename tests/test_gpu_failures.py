@@ -101,3 +101,21 @@ def test_driver_rejects_unknown_algo_and_shape(native):
     assert r.returncode == 2 and "unknown -algo" in r.stderr
     r = _main(native, "-algo=gcoospdm", "-nRowsA=64", "-nColsA=64", "-nRowsB=64", "-nColsB=63")
     assert r.returncode == 2
+
+
+def test_reference_algorithm_baseline_bit_identical(native, torch):
+    """The GPU restatement of the reference algorithm (a timing baseline) gives
+    the same FP32 bits as the library, end to end and kernel only."""
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense_torch(90, 1001, 700, 0.05, device="cuda")
+    B = dg.dense_pm1_torch(90, 5, 700, 300, device="cuda")
+    ours = native.GcooHandle(A).build().spdm(B)
+    ref = native.RefAlgoBaseline(A)
+    C1 = torch.empty_like(ours)
+    ref.multiply_by(B, C1)
+    assert torch.equal(C1, ours)
+    ref.build()
+    C2 = torch.zeros_like(ours)
+    ref.run_kernel(B, C2)
+    assert torch.equal(C2, ours)
+    ref.close()
