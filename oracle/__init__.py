@@ -191,3 +191,76 @@ def ref_spdm(g: Gcoo, B: np.ndarray) -> np.ndarray:
     ref().ref_emu_spdm(_arr(g.vals, np.float32), _arr(g.cols, np.int32), _arr(g.rows, np.int32),
                        g.groupIndex, g.nnzPerGroup, g.m, g.k, _arr(B, np.float32), n, Cm)
     return Cm
+
+
+# --- the reference kernels compiled for sm_103a (only where the cubin exists) -
+
+_REFGPU_CUBIN = os.path.join(_HERE, "_ref", "ref_gcoo_sm103a.cubin")
+_REFGPU_RUNNER = os.path.join(_HERE, "_build", "libref_gpu_runner.so")
+_refgpu = None
+
+
+def refgpu_available() -> bool:
+    """The reference's own kernels, compiled from its source into a cubin where
+    the reference tree exists; the runner is built wherever CUDA is."""
+    return os.path.exists(_REFGPU_CUBIN)
+
+
+def refgpu():
+    """Load the runner and the cubin into the current CUDA context."""
+    global _refgpu
+    if _refgpu is None:
+        if not os.path.exists(_REFGPU_RUNNER):
+            build()
+        R = C.CDLL(_REFGPU_RUNNER)
+        R.refgpu_error.restype = C.c_char_p
+        R.refgpu_load.argtypes = [C.c_char_p]
+        R.refgpu_count_scan.argtypes = [C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_uint64, C.c_uint64,
+                                        C.POINTER(C.c_longlong)]
+        R.refgpu_scatter.argtypes = [C.c_int, C.c_uint64, C.c_int, C.c_int] + [C.c_uint64] * 5
+        R.refgpu_spdm.argtypes = [C.c_uint64] * 5 + [C.c_int, C.c_int, C.c_uint64, C.c_int, C.c_uint64]
+        if R.refgpu_load(_REFGPU_CUBIN.encode()) != 0:
+            raise RuntimeError("reference cubin: " + R.refgpu_error().decode())
+        _refgpu = R
+    return _refgpu
+
+
+def _check(rc):
+    if rc != 0:
+        raise RuntimeError("reference kernels: " + refgpu().refgpu_error().decode())
+
+
+def refgpu_convert(dA, cpg: int = 4) -> dict:
+    """The reference conversion on the GPU over a device tensor A (m x k FP32).
+    Returns device tensors groupIndex, nnzPerGroup (nGroup+1 each), vals, rows,
+    cols (nnz each) and nnz."""
+    import torch
+    m, k = int(dA.shape[0]), int(dA.shape[1])
+    ng = (m + cpg - 1) // cpg
+    R = refgpu()
+    gi = torch.zeros(2 * (ng + 1), dtype=torch.int32, device=dA.device)  # one allocation, like the reference
+    nnz = C.c_longlong(0)
+    _check(R.refgpu_count_scan(cpg, dA.data_ptr(), m, k, gi.data_ptr(), gi[ng + 1:].data_ptr(), C.byref(nnz)))
+    n = int(nnz.value)
+    vals = torch.empty(max(n, 1), dtype=torch.float32, device=dA.device)
+    rc = torch.empty(2 * max(n, 1), dtype=torch.int32, device=dA.device)
+    _check(R.refgpu_scatter(cpg, dA.data_ptr(), m, k, gi.data_ptr(), gi[ng + 1:].data_ptr(), vals.data_ptr(),
+                            rc.data_ptr(), rc[max(n, 1):].data_ptr()))
+    return {"groupIndex": gi[:ng + 1], "nnzPerGroup": gi[ng + 1:], "vals": vals[:n], "rows": rc[:n],
+            "cols": rc[max(n, 1):max(n, 1) + n], "nnz": n, "m": m, "k": k, "cpg": cpg,
+            "_keep": (gi, vals, rc)}
+
+
+def refgpu_column_per_group() -> int:
+    return int(refgpu().refgpu_column_per_group())
+
+
+def refgpu_spdm(g: dict, dB, dC) -> None:
+    """The reference multiply kernel on the GPU (compiled CPG and BS)."""
+    if g["cpg"] != refgpu_column_per_group():
+        raise ValueError("the reference multiply is compiled for COLUMN_PER_GROUP=%d" % refgpu_column_per_group())
+    gi, vals, rc = g["_keep"]
+    n = int(dB.shape[1])
+    nn = max(g["nnz"], 1)
+    _check(refgpu().refgpu_spdm(vals.data_ptr(), rc[nn:].data_ptr(), rc.data_ptr(), g["groupIndex"].data_ptr(),
+                                g["nnzPerGroup"].data_ptr(), g["m"], g["k"], dB.data_ptr(), n, dC.data_ptr()))
