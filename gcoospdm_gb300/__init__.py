@@ -291,6 +291,53 @@ class GcooBatch:
             pass
 
 
+class GcooSession:
+    """mutiplyBy from HOST buffers (gcoo_session_*): A moves in row panels, each
+    panel converted and multiplied as soon as it and B are on the device, C
+    panels copied back while later panels are in flight. Same bits as
+    GcooHandle.multiply_by. Host tensors should be pinned for full link speed."""
+
+    def __init__(self, rows_per_group: int = 4, panel_rows: int = 0, **params):
+        p = make_params(rows_per_group=rows_per_group, **params)
+        self._s = C.c_void_p()
+        check(lib().gcoo_session_create(C.byref(self._s), C.byref(p), int(panel_rows)))
+
+    def multiply(self, A, B, Cout=None, stream=None):
+        """C = A x B with A, B, C CPU tensors (float32, row-major contiguous)."""
+        torch = _torch()
+        for t, name in ((A, "A"), (B, "B")):
+            if t.device.type != "cpu" or t.dtype != torch.float32 or not t.is_contiguous() or t.dim() != 2:
+                raise ValueError(f"{name} must be a contiguous 2-D float32 host tensor")
+        m, k = int(A.shape[0]), int(A.shape[1])
+        if int(B.shape[0]) != k:
+            raise ValueError("B must have k rows")
+        n = int(B.shape[1])
+        if Cout is None:
+            Cout = torch.empty((m, n), dtype=torch.float32, pin_memory=A.is_pinned())
+        if Cout.device.type != "cpu" or tuple(Cout.shape) != (m, n) or not Cout.is_contiguous() \
+                or Cout.dtype != torch.float32:
+            raise ValueError("C must be a contiguous m x n float32 host tensor")
+        check(lib().gcoo_session_multiply(self._s, C.c_void_p(A.data_ptr()), m, k, C.c_void_p(B.data_ptr()), n,
+                                          C.c_void_p(Cout.data_ptr()), _stream_ptr(stream)))
+        return Cout
+
+    def stats(self) -> dict:
+        launches, panels = C.c_int32(), C.c_int32()
+        check(lib().gcoo_session_stats(self._s, C.byref(launches), C.byref(panels)))
+        return {"launches": int(launches.value), "panels": int(panels.value)}
+
+    def close(self):
+        if getattr(self, "_s", None) and self._s.value:
+            lib().gcoo_session_destroy(self._s)
+            self._s = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def autotune_save(path: str):
     check(lib().gcoo_autotune_save(path.encode()))
 

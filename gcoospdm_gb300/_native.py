@@ -34,6 +34,7 @@ EXPORTS = (
     "gcoo_device_status",
     "gcoo_convert_count", "gcoo_convert_count_static", "gcoo_convert_scatter", "gcoo_spdm_view", "gcoo_error_norm",
     "gcoo_batch_create", "gcoo_batch_run", "gcoo_batch_launches", "gcoo_batch_destroy",
+    "gcoo_session_create", "gcoo_session_multiply", "gcoo_session_stats", "gcoo_session_destroy",
     "gcoo_autotune", "gcoo_autotune_save", "gcoo_autotune_load", "gcoo_autotune_clear",
 )
 
@@ -111,6 +112,10 @@ def _declare(L) -> None:
         "gcoo_batch_run": (st, [vp, vp]),
         "gcoo_batch_launches": (st, [vp, C.POINTER(i32)]),
         "gcoo_batch_destroy": (st, [vp]),
+        "gcoo_session_create": (st, [C.POINTER(vp), C.POINTER(Params), i64]),
+        "gcoo_session_multiply": (st, [vp, vp, i64, i64, vp, i64, vp, vp]),
+        "gcoo_session_stats": (st, [vp, C.POINTER(i32), C.POINTER(i32)]),
+        "gcoo_session_destroy": (st, [vp]),
         "gcoo_autotune": (st, [vp, vp, i64, vp, vp, C.POINTER(Params)]),
         "gcoo_autotune_save": (st, [C.c_char_p]),
         "gcoo_autotune_load": (st, [C.c_char_p]),

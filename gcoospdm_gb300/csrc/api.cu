@@ -224,7 +224,16 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
     GCOO_CUDA(cudaMemsetAsync(h->status.ptr, 0, sizeof(uint32_t), st));
     int64_t *d_total = h->scratch.ptr + sc; // [0] total nnz, [1] longest row
     GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, sizeof(int64_t), st));
-    GCOO_CUDA(launch_row_count(h->dA, h->m, h->k, h->row_ptr.ptr, st));
+    const int32_t cpg = h->p.rows_per_group;
+    const bool tiled = tiled_convert_ok(h->dA, h->m, h->k, cpg);
+    if (tiled) {
+        if (!h->tile_cnt.ensure(static_cast<size_t>(h->m * conv_segments(h->k))))
+            return fail(GCOO_ERROR_ALLOC, "device allocation of the tile counts failed");
+        GCOO_CUDA(launch_tile_count(h->dA, h->m, h->k, cpg, h->tile_cnt.ptr, st));
+        GCOO_CUDA(launch_tile_prefix(h->tile_cnt.ptr, h->m, h->k, h->row_ptr.ptr, st));
+    } else {
+        GCOO_CUDA(launch_row_count(h->dA, h->m, h->k, h->row_ptr.ptr, st));
+    }
     GCOO_CUDA(launch_row_scan(h->row_ptr.ptr, h->m, h->p.rows_per_group, h->group_index(), h->nnz_per_group(),
                               d_total, h->scratch.ptr, h->status.ptr, st));
     GCOO_CUDA(launch_row_max(h->row_ptr.ptr, h->m, d_total + 1, st));
@@ -241,8 +250,12 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
     // rows and cols live in one block, as in the reference (src/ShGCOOSpDM.cu:95-97)
     int32_t *rows = h->rc.ptr;
     int32_t *cols = h->rc.ptr + nnz;
-    GCOO_CUDA(launch_scatter(h->dA, h->m, h->k, h->p.rows_per_group, h->group_index(), h->row_ptr.ptr,
-                             h->vals.ptr, rows, cols, h->packed.ptr, st));
+    if (tiled)
+        GCOO_CUDA(launch_tile_scatter(h->dA, h->m, h->k, cpg, h->tile_cnt.ptr, h->group_index(), h->row_ptr.ptr,
+                                      h->vals.ptr, rows, cols, h->packed.ptr, st));
+    else
+        GCOO_CUDA(launch_scatter(h->dA, h->m, h->k, cpg, h->group_index(), h->row_ptr.ptr, h->vals.ptr, rows,
+                                 cols, h->packed.ptr, st));
     h->nnz = total;
     h->built = true;
     if (h->tc)

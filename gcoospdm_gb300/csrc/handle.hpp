@@ -31,6 +31,7 @@ struct gcoo_handle {
     gcoo::DevBuf<float> vals;        // reference GCOO order
     gcoo::DevBuf<int32_t> rc;        // rows[nnz] | cols[nnz]
     gcoo::DevBuf<gcoo::Entry> packed; // row order, nnz + 2 (16-byte padded)
+    gcoo::DevBuf<int32_t> tile_cnt;  // per-(row, column tile) counts of the tiled conversion
     gcoo::DevBuf<int64_t> scratch;   // scan block sums (+1) and the total
     gcoo::DevBuf<uint32_t> status;   // device status word
     gcoo::DevBuf<double> norm;       // error-norm accumulators

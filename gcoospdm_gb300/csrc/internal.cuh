@@ -98,6 +98,20 @@ cudaError_t launch_scatter(const float *A, int64_t m, int64_t k, int32_t rows_pe
                            const int32_t *group_index, const int32_t *row_ptr, float *vals,
                            int32_t *rows, int32_t *cols, Entry *packed, cudaStream_t st);
 
+// ---- tiled conversion (convert_tiled.cu): a warp per (group, 128-column segment)
+int64_t conv_segments(int64_t k); // segments per row: the count array is m x conv_segments(k)
+// The tiled kernels need k % 4 == 0, a 16-byte aligned A and rows_per_group <= 8.
+bool tiled_convert_ok(const float *A, int64_t m, int64_t k, int32_t cpg);
+// cnt[r * S + s] = nonzeros of row r in column segment s (S = conv_segments(k)).
+cudaError_t launch_tile_count(const float *A, int64_t m, int64_t k, int32_t cpg, int32_t *cnt,
+                              cudaStream_t st);
+// cnt rows -> exclusive prefix over segments (in place); row totals -> row_cnt[0..m).
+cudaError_t launch_tile_prefix(int32_t *cnt, int64_t m, int64_t k, int32_t *row_cnt, cudaStream_t st);
+// Same outputs as launch_scatter, from the segment prefixes.
+cudaError_t launch_tile_scatter(const float *A, int64_t m, int64_t k, int32_t cpg, const int32_t *pref,
+                                const int32_t *group_index, const int32_t *row_ptr, float *vals,
+                                int32_t *rows, int32_t *cols, Entry *packed, cudaStream_t st);
+
 // ---- FP32 multiply (spdm_fp32.cu) ------------------------------------------------------
 struct LaunchShape {
     int vec;       // columns per thread (1, 2, 4)

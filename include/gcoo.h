@@ -255,6 +255,34 @@ gcoo_status gcoo_batch_launches(const gcoo_batch *b, int32_t *launches);
 
 gcoo_status gcoo_batch_destroy(gcoo_batch *b);
 
+/* ---- multiply from host buffers, pipelined ------------------------------------ */
+
+/* No counterpart in the reference, whose plugin takes device buffers
+ * (src/ShGemm.h:11-14) and whose driver copies A and B in and C out around it
+ * (src/main.cu:23-40,86-89). A session is mutiplyBy for operands that live in
+ * host memory: A is moved in row panels, each panel converted and multiplied
+ * as soon as it and B are on the device, and each panel of C copied back while
+ * the next panels are in flight (copy-in, compute and copy-out on their own
+ * streams). The FP32 results are the same bits as gcoo_multiply_by. */
+typedef struct gcoo_session gcoo_session;
+
+/* panel_rows: rows of A per panel (rounded up to rows_per_group); 0 picks
+ * about 16 panels. Allocates nothing until the first multiply. */
+gcoo_status gcoo_session_create(gcoo_session **out, const gcoo_params *params, int64_t panel_rows);
+
+/* C = A x B, A m x k, B k x n, C m x n, all row-major FP32 in HOST memory
+ * (page-locked memory moves at full link speed; pageable memory works, more
+ * slowly). Device buffers grow to the largest call and are reused, so a
+ * steady loop allocates nothing. Work is ordered after what was queued on
+ * `stream` before the call; returns once C is complete on the host. */
+gcoo_status gcoo_session_multiply(gcoo_session *s, const float *hA, int64_t m, int64_t k, const float *hB,
+                                  int64_t n, float *hC, void *stream);
+
+/* Kernel launches and panels of the last gcoo_session_multiply. */
+gcoo_status gcoo_session_stats(const gcoo_session *s, int32_t *launches, int32_t *panels);
+
+gcoo_status gcoo_session_destroy(gcoo_session *s);
+
 /* ---- autotuner ---------------------------------------------------------------- */
 
 /* Times the candidate (vec, warps, col_warps) settings for this handle at
