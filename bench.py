@@ -363,6 +363,14 @@ def run_ours(args, rank, world, local, pg):
     if prof and prof.get("n") == n and abs(prof.get("sparsity", 0) - args.sparsity) < 1e-9:
         traffic = prof.get("dram_bytes_per_launch")
     fma_peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    # The binding path: one 4-byte B value per FMA comes through L2 (ncu: L2
+    # reads per launch, and their share of the L2 peak at the ncu duration).
+    l2_path = None
+    if traffic and prof.get("l2_read_bytes_per_launch"):
+        l2b = prof["l2_read_bytes_per_launch"]
+        l2_path = {"l2_read_bytes_per_launch": l2b, "achieved_gbs": round(l2b / t_spdm / 1e9, 1),
+                   "ncu_l2_throughput_pct_of_peak": prof.get("l2_throughput_pct_of_peak"),
+                   "note": "L2 reads from one ncu capture; achieved = those bytes / this run's kernel time"}
     # conversion alone (build: count + scan + scatter, one readback)
     for _ in range(2):
         h.build()
@@ -453,6 +461,7 @@ def run_ours(args, rank, world, local, pg):
                      "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
                      "kernel": "spdm_fp32_kernel", "algorithmic_bytes": alg_bytes,
                      "kernel_ms": round(t_spdm * 1e3, 4), "peak_source": peak_kind},
+        "l2_path": l2_path,
         "fma_roofline": {"achieved_tflops": round(flop / t_spdm / 1e12, 3), "nominal_peak_tflops": round(fma_peak, 1),
                          "frac": round(flop / t_spdm / 1e12 / fma_peak, 4)},
         "spdm_only_gflops": round(flop / t_spdm / 1e9, 3),
