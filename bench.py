@@ -641,6 +641,7 @@ def run_sweep(args):
     import gcoospdm_gb300 as g
     from gcoospdm_gb300 import datagen as dg
     dev = torch.device("cuda", 0)
+    peaks, _ = measured_peaks()
     for n in (2048, 4096, 8192, 16384):
         B = dg.dense_pm1_torch(n, 5, n, n, device=dev)
         Cd = torch.empty(n, n, device=dev)
@@ -654,7 +655,9 @@ def run_sweep(args):
             alg = 12 * nnz + 8 * (n // 4 + 1) + 8 * n * n
             print(json.dumps({"n": n, "sparsity": s, "nnz": nnz, "convert_ms": round(conv, 4),
                               "spdm_ms": round(ms, 4), "spdm_gflops": round(2.0 * nnz * n / ms / 1e6, 1),
-                              "spdm_gbps": round(alg / ms / 1e6, 1), "multiply_by_ms": round(e2e, 4),
+                              "spdm_gbps": round(alg / ms / 1e6, 1),
+                              "hbm_frac": round(alg / ms / 1e6 / peaks["hbm_gbs"], 4),
+                              "l2_read_gbps": round(4.0 * nnz * n / ms / 1e6, 1), "multiply_by_ms": round(e2e, 4),
                               "multiply_by_gflops": round(2.0 * nnz * n / e2e / 1e6, 1),
                               "rel_fro_vs_fp64": h.error_norm(B, Cd) if n <= 4096 else None}), flush=True)
             del A, h

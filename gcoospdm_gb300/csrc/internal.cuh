@@ -119,6 +119,7 @@ struct LaunchShape {
     int col_warps; // warps side by side on one row
     int depth;     // 1: plain batches, 2: B loads of the next batch in flight
     int rows;      // rows per CTA
+    int col_iters = 1; // column tiles each warp walks with one staging of its group's entries
 };
 LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, int64_t max_row,
                        uintptr_t b_addr, uintptr_t c_addr);

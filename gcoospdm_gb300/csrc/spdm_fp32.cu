@@ -127,12 +127,17 @@ __device__ __forceinline__ void row_chain(const Entry *__restrict__ s, int cnt, 
 
 // MAXT bounds the CTA size (rows_per_group * col_warps warps); the 1024-thread
 // variant (rows_per_group 32) unrolls less to stay within 64 registers.
-template <int V, int MAXT, bool PIPE>
+// col_iters > 1 (only when every group's entries fit one staging chunk): each
+// warp walks col_iters column tiles, col_warps tiles apart, reusing the
+// staged entries, so short rows do not pay one staging per tile.
+template <int V, int MAXT, bool PIPE, bool MULTI>
 __global__ void __launch_bounds__(MAXT)
 spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ row_ptr, int64_t m,
                  int32_t cpg, const float *__restrict__ B, int64_t n, float *__restrict__ C,
-                 int32_t col_warps, uint32_t *__restrict__ status)
+                 int32_t col_warps, int32_t col_iters, uint32_t *__restrict__ status)
 {
+    if (!MULTI)
+        col_iters = 1;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     Entry *s_nz = reinterpret_cast<Entry *>(smem + 128);
@@ -143,7 +148,9 @@ spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ r
     const int64_t r_end = r0 + cpg < m ? r0 + cpg : m;
     const int64_t row = r0 + slot;
     const bool has_row = slot < cpg && row < r_end;
-    const int64_t j = (static_cast<int64_t>(blockIdx.y) * col_warps + sub) * (32 * V) + static_cast<int64_t>(lane) * V;
+    const int64_t tile_stride = static_cast<int64_t>(col_warps) * (32 * V);
+    const int64_t j = (static_cast<int64_t>(blockIdx.y) * col_iters * col_warps + sub) * (32 * V) +
+                      static_cast<int64_t>(lane) * V;
     const bool has_col = j < n;
 
     const int64_t gs = row_ptr[r0];
@@ -195,6 +202,23 @@ spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ r
     }
     if (has_row && has_col && ok)
         Vec<V>::store(C + row * n + j, acc);
+    // further column tiles of the same rows: the (single) chunk is still staged
+    if (MULTI && col_iters > 1 && nchunks == 1 && ok && has_row) {
+        const int64_t a0 = gs & ~static_cast<int64_t>(1);
+        const Entry *s_row = s_nz + (rs - a0);
+        const int cnt = static_cast<int>(re - rs);
+        for (int it = 1; it < col_iters; ++it) {
+            const int64_t jt = j + it * tile_stride;
+            if (jt >= n)
+                break;
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                acc[v] = 0.0f;
+            if (cnt > 0)
+                row_chain<V, (MAXT > 512 ? 4 : 8), PIPE>(s_row, cnt, B + jt, n, acc);
+            Vec<V>::store(C + row * n + jt, acc);
+        }
+    }
 }
 
 // Multiply straight from reference-layout arrays (entries of a group in
@@ -228,6 +252,18 @@ spdm_view_kernel(const float *__restrict__ vals, const int32_t *__restrict__ row
         for (int r = 0; r < cpg && r0 + r < m; ++r)
             C[(r0 + r) * n + j] = s_acc[r * kViewThreads + threadIdx.x];
     }
+}
+
+int device_sms()
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+            sms = 152;
+    }
+    return sms;
 }
 
 } // namespace
@@ -272,6 +308,21 @@ LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, 
     s.col_warps = cw;
     s.warps = cw * cpg;
     s.depth = p.depth > 0 ? p.depth : (skewed ? 2 : 1);
+    // Short rows: one staging of a group's entries serves several column
+    // tiles (about 64 entries per warp), when every group fits one chunk.
+    s.col_iters = 1;
+    if (max_row > 0 && max_row * static_cast<int64_t>(s.rows) + 2 <= kChunk) {
+        const int64_t tile = static_cast<int64_t>(s.col_warps) * 32 * s.vec;
+        const int64_t ny = (n + tile - 1) / tile;
+        const double per_row = mean > 1.0 ? mean : 1.0;
+        int64_t ci = static_cast<int64_t>(64.0 / per_row);
+        // keep about four waves of CTAs (6 resident per SM) for latency hiding
+        const int64_t groups = (m + s.rows - 1) / s.rows;
+        const int64_t by_grid = groups * ny / (static_cast<int64_t>(device_sms()) * 24);
+        ci = ci > by_grid ? by_grid : ci;
+        ci = ci < 1 ? 1 : (ci > ny ? ny : ci);
+        s.col_iters = static_cast<int>(ci > 64 ? 64 : ci);
+    }
     return s;
 }
 
@@ -280,7 +331,7 @@ cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_
 {
     const int32_t cpg = s.rows; // rows per CTA (any value gives the same fmaf chains)
     const int64_t ng = (m + cpg - 1) / cpg;
-    const int64_t tile = static_cast<int64_t>(s.col_warps) * 32 * s.vec;
+    const int64_t tile = static_cast<int64_t>(s.col_warps) * 32 * s.vec * (s.col_iters > 1 ? s.col_iters : 1);
     const int64_t ny = (n + tile - 1) / tile;
     if (ng <= 0 || ny <= 0)
         return cudaSuccess;
@@ -289,7 +340,14 @@ cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_
     dim3 grid(static_cast<unsigned>(ng), static_cast<unsigned>(ny));
     const int threads = s.warps * 32;
 #define GCOO_FP32_LAUNCH(V, T, P)                                                                       \
-    spdm_fp32_kernel<V, T, P><<<grid, threads, kSmemBytes, st>>>(packed, row_ptr, m, cpg, B, n, C, s.col_warps, status)
+    do {                                                                                                \
+        if (s.col_iters > 1)                                                                            \
+            spdm_fp32_kernel<V, T, P, true><<<grid, threads, kSmemBytes, st>>>(                         \
+                packed, row_ptr, m, cpg, B, n, C, s.col_warps, s.col_iters, status);                    \
+        else                                                                                            \
+            spdm_fp32_kernel<V, T, P, false><<<grid, threads, kSmemBytes, st>>>(                        \
+                packed, row_ptr, m, cpg, B, n, C, s.col_warps, 1, status);                              \
+    } while (0)
 #define GCOO_FP32_VEC(T, P)                                                                             \
     do {                                                                                                \
         if (s.vec == 4) GCOO_FP32_LAUNCH(4, T, P);                                                      \
