@@ -125,6 +125,48 @@ __device__ __forceinline__ void row_chain(const Entry *__restrict__ s, int cnt, 
     }
 }
 
+// One row's chain over two column tiles at once (same entries, same fmaf
+// order per element as row_chain): U entries per batch, 2U B loads in flight.
+template <int V, int U>
+__device__ __forceinline__ void row_chain_pair(const Entry *__restrict__ s, int cnt, const float *__restrict__ Ba,
+                                               const float *__restrict__ Bb, int64_t n, float (&acc_a)[V],
+                                               float (&acc_b)[V])
+{
+    int i = 0;
+#pragma unroll 1
+    for (; i + U <= cnt; i += U) {
+        Entry e[U];
+        float ba[U][V], bb[U][V];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            e[u] = s[i + u];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            Vec<V>::load(Ba + static_cast<int64_t>(e[u].col) * n, ba[u]);
+            Vec<V>::load(Bb + static_cast<int64_t>(e[u].col) * n, bb[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                acc_a[v] = fmaf(e[u].val, ba[u][v], acc_a[v]);
+                acc_b[v] = fmaf(e[u].val, bb[u][v], acc_b[v]);
+            }
+    }
+#pragma unroll 1
+    for (; i < cnt; ++i) {
+        const Entry e = s[i];
+        float ba[V], bb[V];
+        Vec<V>::load(Ba + static_cast<int64_t>(e.col) * n, ba);
+        Vec<V>::load(Bb + static_cast<int64_t>(e.col) * n, bb);
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            acc_a[v] = fmaf(e.val, ba[v], acc_a[v]);
+            acc_b[v] = fmaf(e.val, bb[v], acc_b[v]);
+        }
+    }
+}
+
 // MAXT bounds the CTA size (rows_per_group * col_warps warps); the 1024-thread
 // variant (rows_per_group 32) unrolls less to stay within 64 registers.
 // col_iters > 1 (only when every group's entries fit one staging chunk): each
@@ -207,7 +249,26 @@ spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ r
         const int64_t a0 = gs & ~static_cast<int64_t>(1);
         const Entry *s_row = s_nz + (rs - a0);
         const int cnt = static_cast<int>(re - rs);
-        for (int it = 1; it < col_iters; ++it) {
+        int it = 1;
+        // very short rows: two tiles at a time, twice the B loads in flight
+        // (longer rows already keep a batch of 8 loads in flight per tile)
+        for (; cnt < 16 && it + 1 < col_iters; it += 2) {
+            const int64_t ja = j + it * tile_stride, jb = ja + tile_stride;
+            if (ja >= n)
+                break;
+            float a2[V], b2[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                a2[v] = b2[v] = 0.0f;
+            if (jb < n)
+                row_chain_pair<V, 4>(s_row, cnt, B + ja, B + jb, n, a2, b2);
+            else if (cnt > 0)
+                row_chain<V, 4, false>(s_row, cnt, B + ja, n, a2);
+            Vec<V>::store(C + row * n + ja, a2);
+            if (jb < n)
+                Vec<V>::store(C + row * n + jb, b2);
+        }
+        for (; it < col_iters; ++it) {
             const int64_t jt = j + it * tile_stride;
             if (jt >= n)
                 break;
@@ -215,7 +276,7 @@ spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ r
             for (int v = 0; v < V; ++v)
                 acc[v] = 0.0f;
             if (cnt > 0)
-                row_chain<V, (MAXT > 512 ? 4 : 8), PIPE>(s_row, cnt, B + jt, n, acc);
+                row_chain<V, (MAXT > 512 ? 4 : 8), false>(s_row, cnt, B + jt, n, acc);
             Vec<V>::store(C + row * n + jt, acc);
         }
     }

@@ -113,6 +113,21 @@ def test_heavy_group_multi_chunk(native, oracle_mod, torch):
     assert same_bits(h.spdm(dev(torch, B)).cpu().numpy(), ref)
 
 
+@pytest.mark.parametrize("n,vec", [(4100, 4), (4102, 2), (4099, 1), (1920, 4)])
+def test_short_rows_walk_several_column_tiles(native, oracle_mod, torch, n, vec):
+    """Short rows (about 2.5 entries) over many groups and a wide, ragged n:
+    each warp walks several column tiles (in pairs, then one) per staging of
+    its group's entries. Same bits as the oracle."""
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense(26, 8192, 512, 0.005)
+    A[5, :] = 0.0  # an empty row inside a walked group
+    B = dg.dense_pm1(26, 5, 512, n)
+    ref = oracle_mod.spdm(oracle_mod.convert(A), B)
+    h = native.GcooHandle(dev(torch, A), vec=vec).build()
+    assert same_bits(h.spdm(dev(torch, B)).cpu().numpy(), ref)
+    assert h.device_status() == 0
+
+
 def test_reference_layout_view_entry(native, oracle_mod, torch, manifest):
     """gcoo_spdm_view on arrays in the reference's own layout."""
     for name in ("readme_800", "n_tail", "empty_groups"):
