@@ -62,11 +62,15 @@ def _view_tensor(ptr, n, typestr):
     return torch.as_tensor(_DevArray(ptr, n, typestr), device="cuda")
 
 
-def make_params(rows_per_group=4, vec=0, warps=0, col_warps=0, engine="auto", depth=0) -> Params:
+FP32_ORDER = {"auto": 0, "rows": 1, "groups": 2}
+
+
+def make_params(rows_per_group=4, vec=0, warps=0, col_warps=0, engine="auto", depth=0, fp32_order="auto") -> Params:
     p = Params()
     check(lib().gcoo_params_default(C.byref(p)))
     p.rows_per_group = rows_per_group
     p.vec, p.warps, p.col_warps, p.depth = vec, warps, col_warps, depth
+    p.fp32_order = FP32_ORDER[fp32_order] if isinstance(fp32_order, str) else int(fp32_order)
     p.engine = ENGINE[engine] if isinstance(engine, str) else int(engine)
     return p
 
@@ -75,14 +79,14 @@ class GcooHandle:
     """One sparse operand: conversion state plus the multiply entry points."""
 
     def __init__(self, A, rows_per_group: int = 4, vec: int = 0, warps: int = 0, col_warps: int = 0,
-                 engine: str = "auto", depth: int = 0):
+                 engine: str = "auto", depth: int = 0, fp32_order: str = "auto"):
         _check_f32(A, "A")
         if A.dim() != 2:
             raise ValueError("A must be 2-D")
         self._A = A  # keeps the dense operand alive while the handle may read it
         self.m, self.k = int(A.shape[0]), int(A.shape[1])
         self._h = C.c_void_p()
-        p = make_params(rows_per_group, vec, warps, col_warps, engine, depth)
+        p = make_params(rows_per_group, vec, warps, col_warps, engine, depth, fp32_order)
         check(lib().gcoo_create(C.byref(self._h), C.c_void_p(A.data_ptr()), self.m, self.k, C.byref(p)))
         self.rows_per_group = rows_per_group
 

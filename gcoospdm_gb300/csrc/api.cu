@@ -92,9 +92,35 @@ static gcoo_status check_n(int64_t n)
     return GCOO_SUCCESS;
 }
 
+// Whether the FP32 multiply walks groups in GCOO order (one B load per column
+// shared by a group's rows) instead of rows: forced by fp32_order, else when
+// the conversion saw at least 1.5 entries per distinct (group, column) pair.
+static bool use_group_order(const gcoo_handle *h)
+{
+    if (h->coo || !group_order_ok(h->p.rows_per_group) || h->p.fp32_order == 1)
+        return false;
+    if (h->p.fp32_order == 2)
+        return true;
+    return h->distinct_cols > 0 && 2 * h->nnz >= 3 * h->distinct_cols;
+}
+
 gcoo_status spdm_fp32(gcoo_handle *h, const float *dB, int64_t n, float *dC, cudaStream_t st,
                       const gcoo_params *override_params)
 {
+    if (!override_params && use_group_order(h)) {
+        // 8 columns per lane (two 16-byte loads: more FMAs per shuffled entry) where n allows
+        int v = n % 8 == 0 ? 8 : 4;
+        const uintptr_t b = reinterpret_cast<uintptr_t>(dB), c = reinterpret_cast<uintptr_t>(dC);
+        if (n % 4 != 0 || (b & 15) || (c & 15))
+            v = (n % 2 != 0 || (b & 7) || (c & 7)) ? 1 : 2;
+        if (h->p.vec > 0 && h->p.vec < v)
+            v = h->p.vec;
+        cudaError_t e = launch_spdm_fp32_group(h->vals.ptr, h->rc.ptr, h->rc.ptr + h->nnz, h->group_index(), h->m,
+                                               h->ng, dB, n, dC, v, st);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "spdm_fp32_group_kernel launch");
+        return GCOO_SUCCESS;
+    }
     gcoo_params p = h->p;
     if (override_params) {
         p = *override_params;
@@ -188,6 +214,10 @@ gcoo_status gcoo_create(gcoo_handle **out, const float *dA, int64_t m, int64_t k
         return fail(GCOO_ERROR_INVALID_VALUE, "unknown engine");
     if (p.depth < 0 || p.depth > 2)
         return fail(GCOO_ERROR_INVALID_VALUE, "depth must be 0, 1 or 2");
+    if (p.fp32_order < 0 || p.fp32_order > 2)
+        return fail(GCOO_ERROR_INVALID_VALUE, "fp32_order must be 0, 1 or 2");
+    if (p.fp32_order == 2 && !group_order_ok(p.rows_per_group))
+        return fail(GCOO_ERROR_UNSUPPORTED, "the group-order FP32 multiply needs rows_per_group 4");
     gcoo_handle *h = new (std::nothrow) gcoo_handle();
     if (!h)
         return fail(GCOO_ERROR_ALLOC, "host allocation of the handle failed");
@@ -219,17 +249,18 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
     }
     const size_t sc = scan_scratch_elems(h->m);
     if (!h->row_ptr.ensure(static_cast<size_t>(h->m) + 1) || !h->groups.ensure(2 * static_cast<size_t>(h->ng + 1)) ||
-        !h->scratch.ensure(sc + 2) || !h->status.ensure(1))
+        !h->scratch.ensure(sc + 3) || !h->status.ensure(1))
         return fail(GCOO_ERROR_ALLOC, "device allocation of the GCOO index arrays failed");
     GCOO_CUDA(cudaMemsetAsync(h->status.ptr, 0, sizeof(uint32_t), st));
-    int64_t *d_total = h->scratch.ptr + sc; // [0] total nnz, [1] longest row
-    GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, sizeof(int64_t), st));
+    int64_t *d_total = h->scratch.ptr + sc; // [0] total nnz, [1] longest row, [2] distinct group columns
+    GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, 2 * sizeof(int64_t), st));
     const int32_t cpg = h->p.rows_per_group;
     const bool tiled = tiled_convert_ok(h->dA, h->m, h->k, cpg);
     if (tiled) {
         if (!h->tile_cnt.ensure(static_cast<size_t>(h->m * conv_segments(h->k))))
             return fail(GCOO_ERROR_ALLOC, "device allocation of the tile counts failed");
-        GCOO_CUDA(launch_tile_count(h->dA, h->m, h->k, cpg, h->tile_cnt.ptr, st));
+        GCOO_CUDA(launch_tile_count(h->dA, h->m, h->k, cpg, h->tile_cnt.ptr,
+                                    reinterpret_cast<unsigned long long *>(d_total + 2), st));
         GCOO_CUDA(launch_tile_prefix(h->tile_cnt.ptr, h->m, h->k, h->row_ptr.ptr, st));
     } else {
         GCOO_CUDA(launch_row_count(h->dA, h->m, h->k, h->row_ptr.ptr, st));
@@ -237,11 +268,12 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
     GCOO_CUDA(launch_row_scan(h->row_ptr.ptr, h->m, h->p.rows_per_group, h->group_index(), h->nnz_per_group(),
                               d_total, h->scratch.ptr, h->status.ptr, st));
     GCOO_CUDA(launch_row_max(h->row_ptr.ptr, h->m, d_total + 1, st));
-    int64_t tot2[2] = {0, 0};
+    int64_t tot2[3] = {0, 0, 0};
     GCOO_CUDA(cudaMemcpyAsync(tot2, d_total, sizeof(tot2), cudaMemcpyDeviceToHost, st));
     GCOO_CUDA(cudaStreamSynchronize(st));
     const int64_t total = tot2[0];
     h->max_row_nnz = tot2[1];
+    h->distinct_cols = tiled ? tot2[2] : 0; // 0: not counted
     if (total < 0 || total > 0x7fffffffLL)
         return fail(GCOO_ERROR_FORMAT, "nnz = " + std::to_string(total) + " exceeds the int32 GCOO format");
     const size_t nnz = static_cast<size_t>(total);

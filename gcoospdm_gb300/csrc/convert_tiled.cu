@@ -57,25 +57,45 @@ __device__ __forceinline__ SegUnit seg_unit(int64_t m, int64_t k, int64_t tiles)
     return u;
 }
 
+// distinct (when not null) accumulates the number of distinct (group,
+// column) pairs, i.e. columns with a nonzero in at least one row of the
+// group; nnz / distinct tells how many rows of a group share a B row.
 template <int CPG>
 __global__ void __launch_bounds__(kTileThreads)
 seg_count_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t tiles, int64_t S,
-                 int32_t *__restrict__ cnt)
+                 int32_t *__restrict__ cnt, unsigned long long *__restrict__ distinct)
 {
+    __shared__ int s_dist[kSegsPerCta];
     const SegUnit u = seg_unit<CPG>(m, k, tiles);
-    if (!u.live)
-        return; // whole warp: the segment lies past the row end
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float4 v[CPG];
 #pragma unroll
     for (int r = 0; r < CPG; ++r)
-        v[r] = (r < u.nrows && u.c < k) ? __ldg(reinterpret_cast<const float4 *>(A + (u.r0 + r) * k + u.c))
-                                        : make_float4(0.f, 0.f, 0.f, 0.f);
+        v[r] = (u.live && r < u.nrows && u.c < k)
+                   ? __ldg(reinterpret_cast<const float4 *>(A + (u.r0 + r) * k + u.c))
+                   : make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t any = 0;
 #pragma unroll
     for (int r = 0; r < CPG; ++r) {
-        const int x = __reduce_add_sync(0xffffffffu, __popc(nz_bits(v[r])));
-        if (lane == r && r < u.nrows)
+        const uint32_t b = nz_bits(v[r]);
+        any |= b;
+        const int x = __reduce_add_sync(0xffffffffu, __popc(b));
+        if (u.live && lane == r && r < u.nrows)
             cnt[(u.r0 + r) * S + u.s] = x;
+    }
+    if (distinct) {
+        const int d = __reduce_add_sync(0xffffffffu, __popc(any));
+        if (lane == 0)
+            s_dist[warp] = d;
+        __syncthreads(); // every warp of the CTA reaches this (no early exit above)
+        if (threadIdx.x == 0) {
+            int t = 0;
+#pragma unroll
+            for (int w = 0; w < kSegsPerCta; ++w)
+                t += s_dist[w];
+            if (t)
+                atomicAdd(distinct, static_cast<unsigned long long>(t));
+        }
     }
 }
 
@@ -221,7 +241,8 @@ bool tiled_convert_ok(const float *A, int64_t m, int64_t k, int32_t cpg)
            units < 0x7fffffffLL;
 }
 
-cudaError_t launch_tile_count(const float *A, int64_t m, int64_t k, int32_t cpg, int32_t *cnt, cudaStream_t st)
+cudaError_t launch_tile_count(const float *A, int64_t m, int64_t k, int32_t cpg, int32_t *cnt,
+                              unsigned long long *distinct, cudaStream_t st)
 {
     const int64_t tiles = conv_tiles(k), S = conv_segments(k);
     const int64_t units = ((m + cpg - 1) / cpg) * tiles;
@@ -229,10 +250,10 @@ cudaError_t launch_tile_count(const float *A, int64_t m, int64_t k, int32_t cpg,
         return cudaSuccess;
     const unsigned grid = static_cast<unsigned>(units);
     switch (cpg) {
-    case 1: seg_count_kernel<1><<<grid, kTileThreads, 0, st>>>(A, m, k, tiles, S, cnt); break;
-    case 2: seg_count_kernel<2><<<grid, kTileThreads, 0, st>>>(A, m, k, tiles, S, cnt); break;
-    case 4: seg_count_kernel<4><<<grid, kTileThreads, 0, st>>>(A, m, k, tiles, S, cnt); break;
-    case 8: seg_count_kernel<8><<<grid, kTileThreads, 0, st>>>(A, m, k, tiles, S, cnt); break;
+    case 1: seg_count_kernel<1><<<grid, kTileThreads, 0, st>>>(A, m, k, tiles, S, cnt, distinct); break;
+    case 2: seg_count_kernel<2><<<grid, kTileThreads, 0, st>>>(A, m, k, tiles, S, cnt, distinct); break;
+    case 4: seg_count_kernel<4><<<grid, kTileThreads, 0, st>>>(A, m, k, tiles, S, cnt, distinct); break;
+    case 8: seg_count_kernel<8><<<grid, kTileThreads, 0, st>>>(A, m, k, tiles, S, cnt, distinct); break;
     default: return cudaErrorInvalidValue;
     }
     count_launches(1);

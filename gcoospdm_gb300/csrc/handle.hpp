@@ -25,6 +25,7 @@ struct gcoo_handle {
     bool built = false;
     int64_t nnz = 0;
     int64_t max_row_nnz = 0;
+    int64_t distinct_cols = 0; // (group, column) pairs with a nonzero; 0 when not counted
 
     gcoo::DevBuf<int32_t> row_ptr;   // m + 1 (row counts, then exclusive prefix)
     gcoo::DevBuf<int32_t> groups;    // group_index[ng+1] | nnz_per_group[ng+1]

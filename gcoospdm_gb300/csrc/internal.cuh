@@ -103,8 +103,10 @@ int64_t conv_segments(int64_t k); // segments per row: the count array is m x co
 // The tiled kernels need k % 4 == 0, a 16-byte aligned A and rows_per_group <= 8.
 bool tiled_convert_ok(const float *A, int64_t m, int64_t k, int32_t cpg);
 // cnt[r * S + s] = nonzeros of row r in column segment s (S = conv_segments(k)).
+// distinct (may be null; zeroed by the caller) += columns with a nonzero in
+// at least one row of their group, summed over groups.
 cudaError_t launch_tile_count(const float *A, int64_t m, int64_t k, int32_t cpg, int32_t *cnt,
-                              cudaStream_t st);
+                              unsigned long long *distinct, cudaStream_t st);
 // cnt rows -> exclusive prefix over segments (in place); row totals -> row_cnt[0..m).
 cudaError_t launch_tile_prefix(int32_t *cnt, int64_t m, int64_t k, int32_t *row_cnt, cudaStream_t st);
 // Same outputs as launch_scatter, from the segment prefixes.
@@ -126,6 +128,12 @@ LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, 
 cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_t m, const float *B,
                              int64_t n, float *C, const LaunchShape &s, uint32_t *status,
                              cudaStream_t st);
+// FP32 multiply in GCOO order (spdm_fp32_group.cu): one B load per column
+// shared by a group's rows; groups of 4 rows; vec 1, 2, 4 or 8.
+bool group_order_ok(int32_t rows_per_group);
+cudaError_t launch_spdm_fp32_group(const float *vals, const int32_t *rows, const int32_t *cols,
+                                   const int32_t *group_index, int64_t m, int64_t ng, const float *B,
+                                   int64_t n, float *C, int vec, cudaStream_t st);
 // Longest row (row_ptr[r+1] - row_ptr[r]) into *out (an int64 zeroed by the caller).
 cudaError_t launch_row_max(const int32_t *row_ptr, int64_t m, int64_t *out, cudaStream_t st);
 // Multiply straight from reference-layout GCOO arrays (column-major order

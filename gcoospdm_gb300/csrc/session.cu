@@ -232,7 +232,7 @@ gcoo_status gcoo_session_multiply(gcoo_session *s, const float *hA, int64_t m, i
         // panels start on rows_per_group boundaries, so A + r0 * k keeps A's alignment when k % 4 == 0
         const bool tiled = tiled_convert_ok(Ap, rows, k, cpg);
         if (tiled) {
-            GCOO_CUDA(launch_tile_count(Ap, rows, k, cpg, L.tile_cnt.ptr, L.s));
+            GCOO_CUDA(launch_tile_count(Ap, rows, k, cpg, L.tile_cnt.ptr, nullptr, L.s));
             GCOO_CUDA(launch_tile_prefix(L.tile_cnt.ptr, rows, k, L.row_ptr.ptr, L.s));
         } else {
             GCOO_CUDA(launch_row_count(Ap, rows, k, L.row_ptr.ptr, L.s));

@@ -74,7 +74,11 @@ typedef struct gcoo_params {
     int32_t col_warps;      /* warps side by side on one row: 0 auto        */
     int32_t engine;         /* gcoo_engine for non-FP32 forms               */
     int32_t depth;          /* B-load pipelining: 0 auto, 1 off, 2 on        */
-    int32_t reserved[2];
+    int32_t fp32_order;     /* FP32 multiply walk: 0 auto, 1 rows (packed
+                               row order), 2 groups (GCOO order, one B load
+                               per column shared by a group's rows; groups
+                               of 4 rows). All give the same bits.        */
+    int32_t reserved;
 } gcoo_params;
 
 typedef struct gcoo_handle gcoo_handle;
