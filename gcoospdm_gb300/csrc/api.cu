@@ -92,10 +92,11 @@ static gcoo_status check_n(int64_t n)
     return GCOO_SUCCESS;
 }
 
-// Whether the FP32 multiply walks groups in GCOO order (one B load per column
-// shared by a group's rows) instead of rows: forced by fp32_order, else when
-// the conversion saw at least 1.5 entries per distinct (group, column) pair.
-static bool use_group_order(const gcoo_handle *h)
+// Whether the FP32 multiply (and the BF16 / FP8-B forms on the FMA engine)
+// walks groups in GCOO order (one B load per column shared by a group's rows)
+// instead of rows: forced by fp32_order, else when the conversion saw at
+// least 1.5 entries per distinct (group, column) pair.
+bool group_order_chosen(const gcoo_handle *h)
 {
     if (h->coo || !group_order_ok(h->p.rows_per_group) || h->p.fp32_order == 1)
         return false;
@@ -107,7 +108,7 @@ static bool use_group_order(const gcoo_handle *h)
 gcoo_status spdm_fp32(gcoo_handle *h, const float *dB, int64_t n, float *dC, cudaStream_t st,
                       const gcoo_params *override_params)
 {
-    if (!override_params && use_group_order(h)) {
+    if (!override_params && group_order_chosen(h)) {
         // 8 columns per lane (two 16-byte loads: more FMAs per shuffled entry) where n allows
         int v = n % 8 == 0 ? 8 : 4;
         const uintptr_t b = reinterpret_cast<uintptr_t>(dB), c = reinterpret_cast<uintptr_t>(dC);

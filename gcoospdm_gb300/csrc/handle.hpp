@@ -12,6 +12,13 @@ void destroy_lowp_work(LowpWork *w);
 void destroy_left_plan(LeftPlan *p);
 } // namespace gcoo
 
+struct gcoo_handle;
+namespace gcoo {
+// Whether multiplies walk groups in GCOO order (api.cu): forced by
+// fp32_order, else when the rows of a group share columns.
+bool group_order_chosen(const gcoo_handle *h);
+} // namespace gcoo
+
 struct gcoo_handle {
     const float *dA = nullptr;
     // COO source (gcoo_create_coo): device triplets, not owned

@@ -134,6 +134,12 @@ bool group_order_ok(int32_t rows_per_group);
 cudaError_t launch_spdm_fp32_group(const float *vals, const int32_t *rows, const int32_t *cols,
                                    const int32_t *group_index, int64_t m, int64_t ng, const float *B,
                                    int64_t n, float *C, int vec, cudaStream_t st);
+// The same walk for the BF16 / FP8-B forms on the FMA engine, from B already
+// converted to bf16 or E4M3 (+ per-column scales); n % 8 == 0.
+cudaError_t launch_spdm_lowp_group(const float *vals, const int32_t *rows, const int32_t *cols,
+                                   const int32_t *group_index, int64_t m, int64_t ng, const void *B,
+                                   const float *col_scale, int64_t n, float *C, gcoo_precision prec,
+                                   cudaStream_t st);
 // Longest row (row_ptr[r+1] - row_ptr[r]) into *out (an int64 zeroed by the caller).
 cudaError_t launch_row_max(const int32_t *row_ptr, int64_t m, int64_t *out, cudaStream_t st);
 // Multiply straight from reference-layout GCOO arrays (column-major order

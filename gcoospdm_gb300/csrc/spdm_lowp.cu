@@ -344,11 +344,21 @@ gcoo_status lowp_spdm(gcoo_handle *h, int64_t n, float *dC, gcoo_precision prec,
         cw = 16 / cpg > 0 ? 16 / cpg : 1;
     if (cpg > 16)
         return fail(GCOO_ERROR_UNSUPPORTED, "reduced-precision forms on the FMA engine support rows_per_group <= 16");
+    LowpWork *w = h->lowp;
+    if (prec != GCOO_PREC_SPLIT_BF16 && n % 8 == 0 && group_order_chosen(h)) {
+        // rows of a group share columns: decode each B segment once per group
+        cudaError_t e = launch_spdm_lowp_group(
+            h->vals.ptr, h->rc.ptr, h->rc.ptr + h->nnz, h->group_index(), h->m, h->ng,
+            prec == GCOO_PREC_BF16 ? static_cast<const void *>(w->bf.ptr) : static_cast<const void *>(w->f8.ptr),
+            w->scale.ptr, n, dC, prec, st);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "spdm_group_kernel launch (reduced precision)");
+        return GCOO_SUCCESS;
+    }
     const int64_t tile = static_cast<int64_t>(cw) * 32 * V;
     const int64_t ny = (n + tile - 1) / tile;
     dim3 grid(static_cast<unsigned>(h->ng), static_cast<unsigned>(ny));
     const int threads = cw * cpg * 32;
-    LowpWork *w = h->lowp;
     if (prec == GCOO_PREC_BF16)
         spdm_lowp_kernel<kBF16><<<grid, threads, kSmemBytes, st>>>(h->packed.ptr, h->row_ptr.ptr, h->m, cpg, w->bf.ptr,
                                                                   nullptr, n, dC, cw, h->status.ptr);

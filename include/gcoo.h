@@ -74,10 +74,11 @@ typedef struct gcoo_params {
     int32_t col_warps;      /* warps side by side on one row: 0 auto        */
     int32_t engine;         /* gcoo_engine for non-FP32 forms               */
     int32_t depth;          /* B-load pipelining: 0 auto, 1 off, 2 on        */
-    int32_t fp32_order;     /* FP32 multiply walk: 0 auto, 1 rows (packed
-                               row order), 2 groups (GCOO order, one B load
-                               per column shared by a group's rows; groups
-                               of 4 rows). All give the same bits.        */
+    int32_t fp32_order;     /* walk of the FP32 multiply and of the BF16 /
+                               FP8-B forms on the FMA engine: 0 auto, 1 rows
+                               (packed row order), 2 groups (GCOO order, one
+                               B load per column shared by a group's rows;
+                               groups of 4 rows). Both give the same bits. */
     int32_t reserved;
 } gcoo_params;
 

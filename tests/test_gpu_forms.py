@@ -54,6 +54,33 @@ def test_bf16_fma_engine_bit_identical_to_rounded_chain(native, oracle_mod, torc
     assert not h.query_engine("bf16")
 
 
+@pytest.mark.parametrize("n", [512, 1000, 2048])
+def test_group_walk_of_reduced_forms_identical_to_row_walk(native, oracle_mod, torch, n):
+    """BF16 and FP8-B on the FMA engine over a block-clustered A: the GCOO-order
+    walk (chosen automatically there) and the row walk give the same bits, and
+    BF16 equals the oracle's rounded chain."""
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.block_dense(33, 1003, 768, 0.3)
+    B = dg.dense_pm1(33, 5, 768, n)
+    dA, dB = dev(torch, A), dev(torch, B)
+    g = oracle_mod.convert(A)
+    C64 = oracle_mod.spdm_f64(g, B)
+    for prec in ("bf16", "fp8_b"):
+        if prec == "fp8_b" and n % 16:
+            continue  # the FP8-B form wants n % 16 == 0
+        got = {}
+        for order in ("auto", "groups", "rows"):
+            h = native.GcooHandle(dA, engine="cuda_core", fp32_order=order).build()
+            got[order] = h.spdm(dB, prec=prec).cpu().numpy()
+        assert np.array_equal(got["auto"].view(np.uint32), got["rows"].view(np.uint32)), prec
+        assert np.array_equal(got["groups"].view(np.uint32), got["rows"].view(np.uint32)), prec
+        assert rel_fro(got["groups"], C64) <= (1e-2 if prec == "bf16" else 5e-2)
+        if prec == "bf16":
+            gr = oracle_mod.Gcoo(g.m, g.k, g.cpg, g.groupIndex, g.nnzPerGroup, bf16_round(g.vals), g.rows, g.cols)
+            ref = oracle_mod.spdm(gr, bf16_round(B))
+            assert np.array_equal(got["groups"].view(np.uint32), ref.view(np.uint32))
+
+
 def test_split_bf16_fma_engine_fp32_level(native, torch, problem):
     A, B, g, C64 = problem
     h = native.GcooHandle(dev(torch, A), engine="cuda_core").build()
