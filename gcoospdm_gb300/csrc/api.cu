@@ -5,6 +5,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <string>
@@ -250,13 +251,60 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
     }
     const size_t sc = scan_scratch_elems(h->m);
     if (!h->row_ptr.ensure(static_cast<size_t>(h->m) + 1) || !h->groups.ensure(2 * static_cast<size_t>(h->ng + 1)) ||
-        !h->scratch.ensure(sc + 3) || !h->status.ensure(1))
+        !h->scratch.ensure(sc + 4) || !h->status.ensure(1))
         return fail(GCOO_ERROR_ALLOC, "device allocation of the GCOO index arrays failed");
     GCOO_CUDA(cudaMemsetAsync(h->status.ptr, 0, sizeof(uint32_t), st));
-    int64_t *d_total = h->scratch.ptr + sc; // [0] total nnz, [1] longest row, [2] distinct group columns
-    GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, 2 * sizeof(int64_t), st));
+    // [0] total nnz, [1] longest row, [2] distinct group columns, [3] one-pass status
+    int64_t *d_total = h->scratch.ptr + sc;
+    GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, 3 * sizeof(int64_t), st));
     const int32_t cpg = h->p.rows_per_group;
     const bool tiled = tiled_convert_ok(h->dA, h->m, h->k, cpg);
+    // One read of A when the entry arrays of an earlier build have room (a
+    // steady loop of mutiplyBy / build); otherwise, or if they turn out too
+    // small, the two-pass path below converts and sizes them exactly.
+    const int64_t cap = std::min<int64_t>(static_cast<int64_t>(h->vals.count),
+                                          std::min<int64_t>(static_cast<int64_t>(h->rc.count / 2),
+                                                            static_cast<int64_t>(h->cols_tmp.count)));
+    if (tiled && h->vals.ptr && h->cols_tmp.ptr && cap > 0 && onepass_convert_ok(h->dA, h->m, h->k, cpg)) {
+        const int64_t units = onepass_units(h->m, h->k, cpg);
+        if (!h->tile_cnt.ensure(static_cast<size_t>(h->m * conv_segments(h->k))) ||
+            !h->unit_state.ensure(static_cast<size_t>(units)) || !h->ticket.ensure(1))
+            return fail(GCOO_ERROR_ALLOC, "device allocation of the one-pass conversion state failed");
+        GCOO_CUDA(launch_onepass(h->dA, h->m, h->k, cpg, h->tile_cnt.ptr,
+                                 reinterpret_cast<unsigned long long *>(d_total + 2), h->unit_state.ptr,
+                                 h->ticket.ptr, h->vals.ptr, h->rc.ptr, h->cols_tmp.ptr, cap, h->group_index(), d_total,
+                                 reinterpret_cast<uint32_t *>(d_total + 3), st));
+        GCOO_CUDA(launch_tile_prefix(h->tile_cnt.ptr, h->m, h->k, h->row_ptr.ptr, st));
+        GCOO_CUDA(launch_row_scan(h->row_ptr.ptr, h->m, cpg, nullptr, nullptr, d_total, h->scratch.ptr,
+                                  h->status.ptr, st));
+        GCOO_CUDA(launch_row_max(h->row_ptr.ptr, h->m, d_total + 1, st));
+        int64_t t4[4] = {0, 0, 0, 0};
+        GCOO_CUDA(cudaMemcpyAsync(t4, d_total, sizeof(t4), cudaMemcpyDeviceToHost, st));
+        GCOO_CUDA(cudaStreamSynchronize(st));
+        const int64_t total = t4[0];
+        if (total > 0x7fffffffLL)
+            return fail(GCOO_ERROR_FORMAT, "nnz = " + std::to_string(total) + " exceeds the int32 GCOO format");
+        if (t4[3] == 0 && total >= 0 && total <= cap) {
+            if (!h->packed.ensure(static_cast<size_t>(total) + 2))
+                return fail(GCOO_ERROR_ALLOC, "device allocation of the packed entries failed");
+            // rows and cols live in one block, as in the reference (src/ShGCOOSpDM.cu:95-97)
+            GCOO_CUDA(cudaMemcpyAsync(h->rc.ptr + total, h->cols_tmp.ptr, static_cast<size_t>(total) * sizeof(int32_t),
+                                      cudaMemcpyDeviceToDevice, st));
+            GCOO_CUDA(launch_pack(h->vals.ptr, h->rc.ptr, h->cols_tmp.ptr, h->group_index(), h->nnz_per_group(),
+                                  h->row_ptr.ptr, h->m, cpg, h->packed.ptr, st));
+            h->max_row_nnz = t4[1];
+            h->distinct_cols = t4[2];
+            h->nnz = total;
+            h->built = true;
+            if (h->tc)
+                destroy_tc_plan(h->tc);
+            h->tc = nullptr;
+            destroy_left_plan(h->left);
+            h->left = nullptr;
+            return GCOO_SUCCESS;
+        }
+        GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, 3 * sizeof(int64_t), st));
+    }
     if (tiled) {
         if (!h->tile_cnt.ensure(static_cast<size_t>(h->m * conv_segments(h->k))))
             return fail(GCOO_ERROR_ALLOC, "device allocation of the tile counts failed");
@@ -278,7 +326,10 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
     if (total < 0 || total > 0x7fffffffLL)
         return fail(GCOO_ERROR_FORMAT, "nnz = " + std::to_string(total) + " exceeds the int32 GCOO format");
     const size_t nnz = static_cast<size_t>(total);
-    if (!h->vals.ensure(nnz) || !h->rc.ensure(2 * nnz) || !h->packed.ensure(nnz + 2))
+    // a little room beyond nnz lets later builds of a similar matrix take the one-pass path
+    const size_t room = tiled ? nnz + nnz / 16 + 1024 : nnz;
+    if (!h->vals.ensure(room) || !h->rc.ensure(2 * room) || !h->packed.ensure(nnz + 2) ||
+        (tiled && !h->cols_tmp.ensure(room)))
         return fail(GCOO_ERROR_ALLOC, "device allocation of the GCOO entry arrays failed");
     // rows and cols live in one block, as in the reference (src/ShGCOOSpDM.cu:95-97)
     int32_t *rows = h->rc.ptr;

@@ -39,7 +39,10 @@ struct gcoo_handle {
     gcoo::DevBuf<float> vals;        // reference GCOO order
     gcoo::DevBuf<int32_t> rc;        // rows[nnz] | cols[nnz]
     gcoo::DevBuf<gcoo::Entry> packed; // row order, nnz + 2 (16-byte padded)
-    gcoo::DevBuf<int32_t> tile_cnt;  // per-(row, column tile) counts of the tiled conversion
+    gcoo::DevBuf<int32_t> tile_cnt;  // per-(row, column segment) counts of the tiled conversion
+    gcoo::DevBuf<int32_t> cols_tmp;  // one-pass conversion: cols before nnz is known
+    gcoo::DevBuf<unsigned long long> unit_state; // one-pass conversion: look-back words
+    gcoo::DevBuf<unsigned int> ticket;           // one-pass conversion: unit ticket
     gcoo::DevBuf<int64_t> scratch;   // scan block sums (+1) and the total
     gcoo::DevBuf<uint32_t> status;   // device status word
     gcoo::DevBuf<double> norm;       // error-norm accumulators

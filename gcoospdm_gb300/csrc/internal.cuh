@@ -114,6 +114,23 @@ cudaError_t launch_tile_scatter(const float *A, int64_t m, int64_t k, int32_t cp
                                 const int32_t *group_index, const int32_t *row_ptr, float *vals,
                                 int32_t *rows, int32_t *cols, Entry *packed, cudaStream_t st);
 
+// ---- one-pass conversion (convert_onepass.cu) ----------------------------------------
+// Same arrays as the tiled conversion from one read of A: GCOO arrays written
+// up to `cap` entries (cols into their own array), group_index, the segment
+// counts and the total (d_total[0]); *status gets kStatusOverflow when the
+// arrays were too small and kStatusWaitTimeout when a look-back gave up.
+bool onepass_convert_ok(const float *A, int64_t m, int64_t k, int32_t cpg);
+int64_t onepass_units(int64_t m, int64_t k, int32_t cpg);
+cudaError_t launch_onepass(const float *A, int64_t m, int64_t k, int32_t cpg, int32_t *cnt,
+                           unsigned long long *distinct, unsigned long long *state, unsigned int *ticket,
+                           float *vals, int32_t *rows, int32_t *cols, int64_t cap, int32_t *group_index,
+                           int64_t *d_total, uint32_t *status, cudaStream_t st);
+// Row-ordered packed entries from the GCOO arrays and row pointers, and
+// nnz_per_group from group_index (when not null).
+cudaError_t launch_pack(const float *vals, const int32_t *rows, const int32_t *cols, int32_t *group_index,
+                        int32_t *nnz_per_group, const int32_t *row_ptr, int64_t m, int32_t cpg, Entry *packed,
+                        cudaStream_t st);
+
 // ---- FP32 multiply (spdm_fp32.cu) ------------------------------------------------------
 struct LaunchShape {
     int vec;       // columns per thread (1, 2, 4)

@@ -118,6 +118,65 @@ def test_rebuild_after_change(native, oracle_mod, torch):
     np.testing.assert_array_equal(host(h.export()["cols"]), g.cols)
 
 
+@pytest.mark.parametrize("name", GOLDEN)
+def test_one_pass_rebuild_matches_reference(native, oracle_mod, torch, manifest, name):
+    """A second build of the same handle reads A once (decoupled look-back
+    over column tiles, the row order derived from the GCOO arrays): the same
+    arrays as the fixtures, and the same FP32 product."""
+    entry = manifest["cases"][name]
+    A, B = golden_inputs(entry, name)
+    h = native.GcooHandle(dev(torch, A), rows_per_group=entry["cpg"]).build()
+    C1 = h.spdm(dev(torch, B)).cpu().numpy() if B is not None else None
+    h.build()  # arrays from the first build have room: one pass
+    a = h.export()
+    assert a["nnz"] == entry["nnz"]
+    for f in FIELDS:
+        assert digest(host(a[f])) == entry["digests"][f], f
+    if B is not None:
+        C2 = h.spdm(dev(torch, B)).cpu().numpy()
+        assert np.array_equal(np.isnan(C1), np.isnan(C2))
+        assert np.array_equal(C1[~np.isnan(C1)].view(np.uint32), C2[~np.isnan(C2)].view(np.uint32))
+    assert h.device_status() == 0
+
+
+@pytest.mark.parametrize("m,k,p,cpg", [(1001, 516, 0.05, 4), (4099, 2048, 0.01, 4), (777, 1000, 0.3, 8),
+                                       (513, 4096, 0.002, 2), (300, 64, 0.5, 1), (5, 8, 1.0, 4)])
+def test_one_pass_rebuild_matches_oracle(native, oracle_mod, torch, m, k, p, cpg):
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense(200 + m, m, k, p)
+    B = dg.dense_pm1(200 + m, 5, k, 96)
+    g = oracle_mod.convert(A, cpg)
+    h = native.GcooHandle(dev(torch, A), rows_per_group=cpg).build()
+    h.build()
+    a = h.export()
+    assert a["nnz"] == g.nnz
+    for f in FIELDS:
+        np.testing.assert_array_equal(host(a[f]), getattr(g, f), err_msg=f)
+    ref = oracle_mod.spdm(oracle_mod.convert(A, 4), B)
+    assert np.array_equal(h.spdm(dev(torch, B)).cpu().numpy().view(np.uint32), ref.view(np.uint32))
+
+
+def test_one_pass_capacity_fallback_and_shrink(native, oracle_mod, torch):
+    """Rebuild after A got denser than the arrays allow (the one-pass attempt
+    falls back to the two-pass path) and after it got sparser (one pass)."""
+    from gcoospdm_gb300 import datagen as dg
+    A1 = dg.bernoulli_dense(51, 2000, 1024, 0.01)
+    A2 = dg.bernoulli_dense(52, 2000, 1024, 0.2)
+    A3 = dg.bernoulli_dense(53, 2000, 1024, 0.005)
+    dA = dev(torch, A1)
+    h = native.GcooHandle(dA).build()
+    for A in (A2, A3, A2, A1):
+        dA.copy_(dev(torch, A))
+        h.build()
+        h.build()
+        g = oracle_mod.convert(A)
+        a = h.export()
+        assert a["nnz"] == g.nnz
+        for f in FIELDS:
+            np.testing.assert_array_equal(host(a[f]), getattr(g, f), err_msg=f)
+        assert h.device_status() == 0
+
+
 def test_full_size_properties_8192(native, torch):
     """n=8192, s=0.99: counts equal the dense count, offsets are the exclusive
     prefix, every group is (column, row) sorted, values round-trip."""
