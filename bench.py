@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--no-gpu-baselines", action="store_true",
                     help="skip timing the reference algorithm, cuSPARSE and cuBLAS on the same GPU")
     ap.add_argument("--sweep", action="store_true", help="print the FP32 n x sparsity sweep instead")
-    ap.add_argument("--case", choices=["tc_bf16", "tc_split", "convert", "fp32", "batched", "fp8", "bf16_fma"],
+    ap.add_argument("--case", choices=["tc_bf16", "tc_split", "convert", "fp32", "batched", "fp8", "bf16_fma",
+                                       "fp32_block"],
                     help="run one small case a few times (for profiling) and exit")
     return ap.parse_args()
 
@@ -59,12 +60,12 @@ def run_case(args):
     import gcoospdm_gb300 as g
     from gcoospdm_gb300 import datagen as dg
     dev = torch.device("cuda", 0)
-    if args.case in ("tc_bf16", "tc_split"):
+    if args.case in ("tc_bf16", "tc_split", "fp32_block"):
         m, n = 8192, 1024
         A = dg.block_dense_torch(4096 + 750, m, m, 0.25, device=dev)
         B = dg.dense_pm1_torch(4096, 5, m, n, device=dev)
         h = g.GcooHandle(A).build()
-        prec = "bf16" if args.case == "tc_bf16" else "split_bf16"
+        prec = {"tc_bf16": "bf16", "tc_split": "split_bf16", "fp32_block": "fp32"}[args.case]
         for _ in range(3):
             h.spdm(B, prec=prec)
     elif args.case == "batched":
