@@ -591,8 +591,9 @@ def run_irregular(g, dg, torch, dev, m=65536, n=256, nnz=1_200_000):
 
 def run_gpu_baselines(g, torch, A, B, flop):
     """Same workload through the baselines built for this GPU: the reference's
-    GCOO algorithm restated on the GPU, cuSPARSE SpMM (CSR) and cuBLAS SGEMM on
-    the dense-with-zeros operand. Each: convert+multiply and multiply only."""
+    GCOO algorithm restated on the GPU, cuSPARSE SpMM (CSR), cuBLAS SGEMM on
+    the dense-with-zeros operand, and the reference's auxiliary CSR plugin
+    restated. Each: convert+multiply and multiply only."""
     m, k = A.shape
     n = B.shape[1]
     Cd = torch.empty(m, n, device=A.device)
@@ -608,7 +609,7 @@ def run_gpu_baselines(g, torch, A, B, flop):
         ref.close()
     except Exception as e:
         out["reference_algorithm_gcoo"] = {"error": f"{type(e).__name__}: {e}"}
-    for algo in ("cusparse", "cublas"):
+    for algo in ("cusparse", "cublas", "csr"):
         try:
             b = g.SpGemmBuilder.getShGemmAlgo(A, m, k, algo)
             e2e = _time(torch, lambda: b.mutiplyBy(B, k, n, Cd), reps=3, warm=1)

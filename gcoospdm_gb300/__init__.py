@@ -434,7 +434,7 @@ class ShGCOOSpDM(ShGemm):
 
 
 class _BaselineGemm(ShGemm):
-    """cuBLAS / cuSPARSE plugins of libgcoo_baselines.so (same C = self x A)."""
+    """cuBLAS / cuSPARSE / CSR plugins of libgcoo_baselines.so (same C = self x A)."""
 
     _L = None
 
@@ -525,12 +525,12 @@ class RefAlgoBaseline:
 
 
 class SpGemmBuilder:
-    """src/SpGemmBuilder.h:10-24: "gcoospdm" | "cublas" | "cusparse", else None."""
+    """src/SpGemmBuilder.h:10-24: "gcoospdm" | "cublas" | "cusparse" | "csr", else None."""
 
     @staticmethod
     def getShGemmAlgo(denseMatrix, nRows, nCols, desc):  # noqa: N802
         if desc == "gcoospdm":
             return ShGCOOSpDM(denseMatrix, nRows, nCols)
-        if desc in ("cublas", "cusparse"):
+        if desc in ("cublas", "cusparse", "csr"):
             return _BaselineGemm(desc, denseMatrix, nRows, nCols)
         return None

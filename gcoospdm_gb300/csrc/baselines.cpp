@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <cusparse.h>
 #include <stdio.h>
+#include <string.h>
 
 #include "ShGemm.h"
 
@@ -189,15 +190,20 @@ ShGemm *gcoo_make_cusparse_gemm(float *denseMatrix, int nRows, int nCols)
     return new CusparseGemm(denseMatrix, nRows, nCols);
 }
 
+// baseline_csr.cu: the reference's auxiliary "-algo=csr" plugin
+ShGemm *gcoo_make_csr_gemm(float *denseMatrix, int nRows, int nCols);
+
 extern "C" {
 // C entry points for FFI callers that want the baselines (benchmarks).
 void *gcoo_baseline_create(const char *algo, float *denseMatrix, int nRows, int nCols)
 {
     const char *a = algo ? algo : "";
-    if (a[0] == 'c' && a[1] == 'u' && a[2] == 'b')
+    if (!strcmp(a, "cublas"))
         return gcoo_make_cublas_gemm(denseMatrix, nRows, nCols);
-    if (a[0] == 'c' && a[1] == 'u' && a[2] == 's')
+    if (!strcmp(a, "cusparse"))
         return gcoo_make_cusparse_gemm(denseMatrix, nRows, nCols);
+    if (!strcmp(a, "csr"))
+        return gcoo_make_csr_gemm(denseMatrix, nRows, nCols);
     return 0;
 }
 double gcoo_baseline_multiply_by(void *g, float *A, int nRows, int nCols, float *C)

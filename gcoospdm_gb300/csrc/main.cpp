@@ -84,7 +84,7 @@ int main(int argc, char **argv)
     printf("[Benchmark sparse gemm on GPU (Dense A multiply sparse B] - Starting...\n");
     if (flag_value(argc, argv, "help") || flag_value(argc, argv, "?")) {
         printf("Usage -nRowsA=nRowsA -nColsA=nColsA -nRowsB=nRowsB -nColsB=nColsB\n"
-               "      -sparsity=sparsity (of matrix B) -algo=gcoospdm|cublas|cusparse\n"
+               "      -sparsity=sparsity (of matrix B) -algo=gcoospdm|cublas|cusparse|csr\n"
                "      -kernelonly=0|1 -seed=N -check=0|1 -prec=fp32|bf16|split|fp8 -reps=N\n"
                "nColsB should equal nRowsA\n");
         return 0;
@@ -134,7 +134,7 @@ int main(int argc, char **argv)
 
     ShGemm *g = SpGemmBuilder::getShGemmAlgo(dB, (int)nRowsB, (int)nColsB, algo);
     if (!g) {
-        fprintf(stderr, "unknown -algo=%s (supported: gcoospdm, cublas, cusparse)\n", algo.c_str());
+        fprintf(stderr, "unknown -algo=%s (supported: gcoospdm, cublas, cusparse, csr)\n", algo.c_str());
         return 2;
     }
     ShGCOOSpDM *gc = algo == "gcoospdm" ? static_cast<ShGCOOSpDM *>(g) : nullptr;

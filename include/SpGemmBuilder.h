@@ -8,8 +8,11 @@
  *                                  reference's csrmm2/dense2csr calls no
  *                                  longer exist in CUDA 13;
  *                                  libgcoo_baselines.so)
- *   anything else (including the reference's auxiliary "csr") -> NULL
- * All three compute the same C = self x A (row-major), unlike the reference
+ *   "csr"       -> the reference's auxiliary CSR plugin (src/ShCsrSpGemm.cu:
+ *                                  per-call CSR conversion, one CTA per
+ *                                  row; restated, libgcoo_baselines.so)
+ *   anything else -> NULL
+ * All four compute the same C = self x A (row-major), unlike the reference
  * whose cuSPARSE/cuBLAS plugins computed the transposed orientation.
  */
 #ifndef GCOO_SPGEMMBUILDER_H
@@ -24,6 +27,7 @@ class ShCublasGemm;
 class ShCusparseGemm;
 ShGemm *gcoo_make_cublas_gemm(float *denseMatrix, int nRows, int nCols);
 ShGemm *gcoo_make_cusparse_gemm(float *denseMatrix, int nRows, int nCols);
+ShGemm *gcoo_make_csr_gemm(float *denseMatrix, int nRows, int nCols);
 
 class SpGemmBuilder
 {
@@ -36,6 +40,8 @@ class SpGemmBuilder
             return gcoo_make_cublas_gemm(denseMatrix, nRows, nCols);
         if (desc == "cusparse")
             return gcoo_make_cusparse_gemm(denseMatrix, nRows, nCols);
+        if (desc == "csr")
+            return gcoo_make_csr_gemm(denseMatrix, nRows, nCols);
         return 0;
     }
 };

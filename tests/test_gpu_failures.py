@@ -80,7 +80,7 @@ def _main(native, *args):
     return subprocess.run([native.MAIN_PATH, *args], capture_output=True, text=True, timeout=300)
 
 
-@pytest.mark.parametrize("algo", ["gcoospdm", "cusparse", "cublas"])
+@pytest.mark.parametrize("algo", ["gcoospdm", "cusparse", "cublas", "csr"])
 def test_driver_check_passes(native, algo):
     r = _main(native, "-sparsity=0.9", "-nRowsA=300", "-nColsA=260", "-nRowsB=200", "-nColsB=300",
               f"-algo={algo}", "-check=1", "-reps=3")
@@ -97,7 +97,7 @@ def test_driver_precision_forms(native, prec):
 
 
 def test_driver_rejects_unknown_algo_and_shape(native):
-    r = _main(native, "-algo=csr", "-nRowsA=64", "-nColsA=64", "-nRowsB=64", "-nColsB=64")
+    r = _main(native, "-algo=ell", "-nRowsA=64", "-nColsA=64", "-nRowsB=64", "-nColsB=64")
     assert r.returncode == 2 and "unknown -algo" in r.stderr
     r = _main(native, "-algo=gcoospdm", "-nRowsA=64", "-nColsA=64", "-nRowsB=64", "-nColsB=63")
     assert r.returncode == 2

@@ -193,7 +193,17 @@ def test_plugin_mirror_and_builder(native, torch, manifest):
     C2 = torch.empty_like(C1)
     assert g.runKernelTest(dB, 800, 800, C2) == 0.0
     assert torch.equal(C1, C2)
-    assert native.SpGemmBuilder.getShGemmAlgo(dA, 800, 800, "csr") is None
+    assert native.SpGemmBuilder.getShGemmAlgo(dA, 800, 800, "ell") is None
+    # the reference's auxiliary "csr" plugin (a baseline): the same bits
+    csr = native.SpGemmBuilder.getShGemmAlgo(dA, 800, 800, "csr")
+    C3 = torch.full_like(C1, float("nan"))
+    assert csr.mutiplyBy(dB, 800, 800, C3) == 0.0
+    assert torch.equal(C3, C1)
+    csr.build()
+    C3.fill_(float("nan"))
+    assert csr.runKernelTest(dB, 800, 800, C3) == 0.0
+    assert torch.equal(C3, C1)
+    del csr
     # the other orientation: C = B x self
     assert g.mutiply(dB, 800, 800, C2) == 0.0
     ref = (dB.double() @ dA.double()).float()
