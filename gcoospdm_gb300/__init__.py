@@ -201,6 +201,15 @@ class GcooHandle:
         check(lib().gcoo_query_engine(self._h, PREC[prec], C.byref(t)))
         return bool(t.value)
 
+    def check_arrays(self, stream=None) -> int:
+        """Structural validation of the built arrays on the GPU (gcoo_check_arrays):
+        0 when every invariant holds, else the number of offending groups."""
+        bad = C.c_int64()
+        st = lib().gcoo_check_arrays(self._h, _stream_ptr(stream), C.byref(bad))
+        if st not in (0, 6):
+            check(st)
+        return int(bad.value)
+
     def device_status(self, stream=None) -> int:
         s = C.c_uint32()
         st = lib().gcoo_device_status(self._h, _stream_ptr(stream), C.byref(s))

@@ -30,7 +30,7 @@ EXPORTS = (
     "gcoo_abi_version", "gcoo_status_string", "gcoo_last_error", "gcoo_params_default",
     "gcoo_set_allocator", "gcoo_create", "gcoo_create_coo", "gcoo_build", "gcoo_export", "gcoo_spdm", "gcoo_spdm_ex",
     "gcoo_prepare", "gcoo_multiply_by", "gcoo_destroy", "gcoo_spdm_left", "gcoo_query_engine", "gcoo_kernel_launches",
-    "gcoo_check_bounded_wait",
+    "gcoo_check_bounded_wait", "gcoo_check_arrays",
     "gcoo_device_status",
     "gcoo_convert_count", "gcoo_convert_count_static", "gcoo_convert_scatter", "gcoo_spdm_view", "gcoo_error_norm",
     "gcoo_batch_create", "gcoo_batch_run", "gcoo_batch_launches", "gcoo_batch_destroy",
@@ -102,6 +102,7 @@ def _declare(L) -> None:
         "gcoo_query_engine": (st, [vp, C.c_int, C.POINTER(i32)]),
         "gcoo_kernel_launches": (C.c_uint64, []),
         "gcoo_check_bounded_wait": (st, [C.c_uint64, vp]),
+        "gcoo_check_arrays": (st, [vp, vp, C.POINTER(i64)]),
         "gcoo_device_status": (st, [vp, vp, C.POINTER(C.c_uint32)]),
         "gcoo_convert_count": (st, [vp, i64, i64, i32, vp, vp, C.POINTER(i64), vp]),
         "gcoo_convert_count_static": (st, [vp, i64, i64, i32, vp, vp, C.POINTER(i64), vp]),

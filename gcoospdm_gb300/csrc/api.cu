@@ -10,9 +10,14 @@
 #include <mutex>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "handle.hpp"
 
 namespace gcoo {
+
+NvtxRange::NvtxRange(const char *name) { nvtxRangePushA(name); }
+NvtxRange::~NvtxRange() { nvtxRangePop(); }
 
 // ---- errors --------------------------------------------------------------------
 static thread_local std::string t_last_error;
@@ -234,6 +239,7 @@ gcoo_status gcoo_create(gcoo_handle **out, const float *dA, int64_t m, int64_t k
 
 gcoo_status gcoo_build(gcoo_handle *h, void *stream)
 {
+    NvtxRange nvtx("gcoo_build");
     if (!h)
         return fail(GCOO_ERROR_INVALID_VALUE, "handle is NULL");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -352,6 +358,7 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
 
 gcoo_status gcoo_spdm_left(gcoo_handle *h, const float *dD, int64_t p, float *dC, void *stream)
 {
+    NvtxRange nvtx("gcoo_spdm_left");
     if (!h || !dD || !dC)
         return fail(GCOO_ERROR_INVALID_VALUE, "NULL handle or matrix pointer");
     if (!h->built)
@@ -412,6 +419,7 @@ gcoo_status gcoo_export(const gcoo_handle *h, gcoo_view *out)
 
 gcoo_status gcoo_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, void *stream)
 {
+    NvtxRange nvtx("gcoo_spdm");
     if (!h || !dB || !dC)
         return fail(GCOO_ERROR_INVALID_VALUE, "NULL handle or matrix pointer");
     if (!h->built)
@@ -424,6 +432,7 @@ gcoo_status gcoo_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, voi
 
 gcoo_status gcoo_spdm_ex(gcoo_handle *h, const float *dB, int64_t n, float *dC, gcoo_precision prec, void *stream)
 {
+    NvtxRange nvtx("gcoo_spdm_ex");
     if (!h || !dB || !dC)
         return fail(GCOO_ERROR_INVALID_VALUE, "NULL handle or matrix pointer");
     if (!h->built)
@@ -456,6 +465,7 @@ gcoo_status gcoo_prepare(gcoo_handle *h, int64_t n, gcoo_precision prec, void *s
 
 gcoo_status gcoo_multiply_by(gcoo_handle *h, const float *dB, int64_t n, float *dC, void *stream)
 {
+    NvtxRange nvtx("gcoo_multiply_by");
     if (!h || !dB || !dC)
         return fail(GCOO_ERROR_INVALID_VALUE, "NULL handle or matrix pointer");
     gcoo_status s = check_n(n);

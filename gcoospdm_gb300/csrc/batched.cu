@@ -437,6 +437,7 @@ gcoo_status gcoo_batch_create(gcoo_batch **out, const gcoo_problem *problems, in
 
 gcoo_status gcoo_batch_run(gcoo_batch *b, void *stream)
 {
+    NvtxRange nvtx("gcoo_batch_run");
     if (!b || !b->exec)
         return fail(GCOO_ERROR_INVALID_VALUE, "batch is NULL or not created");
     GCOO_CUDA(cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream)));

@@ -45,6 +45,15 @@ gcoo_status cuda_fail(cudaError_t e, const char *what);
 // Adds n to the process-wide launch counter (gcoo_kernel_launches).
 void count_launches(int n);
 
+// NVTX range over a scope (entry points and the session's phases): visible in
+// profilers that attach an NVTX tool, a no-op otherwise (NVTX3 is header-only).
+struct NvtxRange {
+    explicit NvtxRange(const char *name);
+    ~NvtxRange();
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 // ---- device allocation through the pluggable allocator -----------------------------
 void *dev_alloc(size_t bytes);
 void dev_free(void *p);

@@ -168,6 +168,7 @@ gcoo_status gcoo_session_create(gcoo_session **out, const gcoo_params *params, i
 gcoo_status gcoo_session_multiply(gcoo_session *s, const float *hA, int64_t m, int64_t k, const float *hB,
                                   int64_t n, float *hC, void *stream)
 {
+    NvtxRange nvtx("gcoo_session_multiply");
     if (!s || !hA || !hB || !hC)
         return fail(GCOO_ERROR_INVALID_VALUE, "NULL session or matrix pointer");
     if (m <= 0 || k <= 0 || m >= (int64_t(1) << 31) || k >= (int64_t(1) << 31))

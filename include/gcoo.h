@@ -183,6 +183,16 @@ gcoo_status gcoo_query_engine(gcoo_handle *h, gcoo_precision prec, int32_t *tens
  * up and reported it, as it must; the context stays usable. */
 gcoo_status gcoo_check_bounded_wait(uint64_t limit_ns, void *stream);
 
+/* No counterpart in the reference (it has no checks). Validates a built
+ * handle's arrays on the GPU: group_index / nnz_per_group / row pointers
+ * consistent, entries in (column, row) order inside their group, columns in
+ * [0, k), values nonzero, each row's execution-layout entries in ascending
+ * columns and the same entries as the GCOO arrays. Reads only in bounds,
+ * whatever the arrays hold. Returns GCOO_ERROR_FORMAT and the number of
+ * offending groups in *bad_groups (may be NULL) when any check fails.
+ * Synchronises `stream`. */
+gcoo_status gcoo_check_arrays(gcoo_handle *h, void *stream, int64_t *bad_groups);
+
 /* Number of kernels this library has launched in this process (all
  * handles, all entry points); lets a caller count launches in a region. */
 uint64_t gcoo_kernel_launches(void);

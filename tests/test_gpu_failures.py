@@ -119,3 +119,36 @@ def test_reference_algorithm_baseline_bit_identical(native, torch):
     ref.run_kernel(B, C2)
     assert torch.equal(C2, ours)
     ref.close()
+
+
+def test_check_arrays_accepts_built_handles_and_reports_corruption(native, torch):
+    """gcoo_check_arrays: silent on a built handle (both conversion paths and
+    COO ingestion), and reports each kind of damage written into the arrays
+    (no multiply ever runs on damaged arrays; the check reads in bounds)."""
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense_torch(61, 1001, 700, 0.05, device="cuda")
+    h = native.GcooHandle(A).build()
+    assert h.check_arrays() == 0
+    h.build()  # the one-pass rebuild
+    assert h.check_arrays() == 0
+    r, c = torch.nonzero(A, as_tuple=True)
+    hc = native.GcooHandle.from_coo(r.int().contiguous(), c.int().contiguous(), A[r, c].contiguous(), 1001, 700).build()
+    assert hc.check_arrays() == 0
+    a = h.export()
+
+    def damaged(name, idx, value):
+        t = a[name]
+        old = t[idx].clone()
+        t[idx] = value
+        torch.cuda.synchronize()
+        bad = h.check_arrays()
+        t[idx] = old
+        torch.cuda.synchronize()
+        return bad
+
+    assert damaged("cols", 3, 705) >= 1             # column out of range
+    assert damaged("vals", 10, -0.0) >= 1           # an explicit zero entry
+    assert damaged("rows", 7, 1000) >= 1            # row outside its group
+    assert damaged("groupIndex", 5, 2 ** 30) >= 1   # offset far out of range, never dereferenced
+    assert damaged("cols", 0, int(a["cols"][1]) + 1) >= 1  # (column, row) order broken
+    assert h.check_arrays() == 0                    # everything restored
