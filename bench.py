@@ -49,7 +49,7 @@ def parse():
                     help="skip timing the reference algorithm, cuSPARSE and cuBLAS on the same GPU")
     ap.add_argument("--sweep", action="store_true", help="print the FP32 n x sparsity sweep instead")
     ap.add_argument("--case", choices=["tc_bf16", "tc_split", "convert", "fp32", "batched", "fp8", "bf16_fma",
-                                       "fp32_block"],
+                                       "fp32_block", "convert_irregular"],
                     help="run one small case a few times (for profiling) and exit")
     return ap.parse_args()
 
@@ -71,6 +71,15 @@ def run_case(args):
     elif args.case == "batched":
         res = run_batched(g, dg, torch, dev, count=64)
         print(json.dumps(res))
+    elif args.case == "convert_irregular":
+        # the irregular workload's dense operand (65536^2, 17 GB): a first build, then rebuilds
+        m = 65536
+        rows, cols, vals = dg.zipf_coo(65536, m, m, 1_200_000, alpha=2.0, cap=4096)
+        A = torch.zeros(m, m, device=dev)
+        A[torch.from_numpy(rows).to(dev), torch.from_numpy(cols).to(dev)] = torch.from_numpy(vals).to(dev)
+        h = g.GcooHandle(A)
+        print(json.dumps({"first_build_ms": round(_time(torch, h.build, reps=1, warm=0), 4),
+                          "rebuild_ms": round(_time(torch, h.build, reps=3, warm=0), 4), "nnz": h.nnz}))
     else:
         n = args.size
         A = dg.bernoulli_dense_torch(SEED, n, n, 1.0 - args.sparsity, device=dev)

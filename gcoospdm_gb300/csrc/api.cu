@@ -257,49 +257,50 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
     }
     const size_t sc = scan_scratch_elems(h->m);
     if (!h->row_ptr.ensure(static_cast<size_t>(h->m) + 1) || !h->groups.ensure(2 * static_cast<size_t>(h->ng + 1)) ||
-        !h->scratch.ensure(sc + 4) || !h->status.ensure(1))
+        !h->scratch.ensure(sc + 8) || !h->status.ensure(1))
         return fail(GCOO_ERROR_ALLOC, "device allocation of the GCOO index arrays failed");
     GCOO_CUDA(cudaMemsetAsync(h->status.ptr, 0, sizeof(uint32_t), st));
-    // [0] total nnz, [1] longest row, [2] distinct group columns, [3] one-pass status
+    // [0] total nnz, [1] longest row, [2] distinct group columns, [3] staging status, [4] overflowed tiles
     int64_t *d_total = h->scratch.ptr + sc;
-    GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, 3 * sizeof(int64_t), st));
+    GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, 7 * sizeof(int64_t), st));
     const int32_t cpg = h->p.rows_per_group;
     const bool tiled = tiled_convert_ok(h->dA, h->m, h->k, cpg);
     // One read of A when the entry arrays of an earlier build have room (a
     // steady loop of mutiplyBy / build); otherwise, or if they turn out too
     // small, the two-pass path below converts and sizes them exactly.
-    const int64_t cap = std::min<int64_t>(static_cast<int64_t>(h->vals.count),
-                                          std::min<int64_t>(static_cast<int64_t>(h->rc.count / 2),
-                                                            static_cast<int64_t>(h->cols_tmp.count)));
-    if (tiled && h->vals.ptr && h->cols_tmp.ptr && cap > 0 && onepass_convert_ok(h->dA, h->m, h->k, cpg)) {
-        const int64_t units = onepass_units(h->m, h->k, cpg);
+    const int64_t cap = std::min<int64_t>(static_cast<int64_t>(h->vals.count), static_cast<int64_t>(h->rc.count / 2));
+    if (tiled && h->vals.ptr && h->rc.ptr && cap > 0 && staged_convert_ok(h->dA, h->m, h->k, cpg)) {
+        const int64_t tiles = staged_tiles(h->m, h->k, cpg);
+        const int32_t slot = staged_slot(h->nnz, tiles, cpg);
         if (!h->tile_cnt.ensure(static_cast<size_t>(h->m * conv_segments(h->k))) ||
-            !h->unit_state.ensure(static_cast<size_t>(units)) || !h->ticket.ensure(1))
-            return fail(GCOO_ERROR_ALLOC, "device allocation of the one-pass conversion state failed");
-        GCOO_CUDA(launch_onepass(h->dA, h->m, h->k, cpg, h->tile_cnt.ptr,
-                                 reinterpret_cast<unsigned long long *>(d_total + 2), h->unit_state.ptr,
-                                 h->ticket.ptr, h->vals.ptr, h->rc.ptr, h->cols_tmp.ptr, cap, h->group_index(), d_total,
-                                 reinterpret_cast<uint32_t *>(d_total + 3), st));
+            !h->stage.ensure(static_cast<size_t>(tiles) * static_cast<size_t>(slot)) ||
+            !h->tile_tot.ensure(static_cast<size_t>(tiles)) || !h->over_list.ensure(static_cast<size_t>(tiles)))
+            return fail(GCOO_ERROR_ALLOC, "device allocation of the staged conversion state failed");
+        unsigned long long *over_count = reinterpret_cast<unsigned long long *>(d_total + 4);
+        GCOO_CUDA(launch_stage(h->dA, h->m, h->k, cpg, slot, h->tile_cnt.ptr,
+                               reinterpret_cast<unsigned long long *>(d_total + 2), h->stage.ptr, h->tile_tot.ptr,
+                               h->over_list.ptr, over_count, reinterpret_cast<uint32_t *>(d_total + 3), st));
         GCOO_CUDA(launch_tile_prefix(h->tile_cnt.ptr, h->m, h->k, h->row_ptr.ptr, st));
-        GCOO_CUDA(launch_row_scan(h->row_ptr.ptr, h->m, cpg, nullptr, nullptr, d_total, h->scratch.ptr,
-                                  h->status.ptr, st));
-        GCOO_CUDA(launch_row_max(h->row_ptr.ptr, h->m, d_total + 1, st));
-        int64_t t4[4] = {0, 0, 0, 0};
-        GCOO_CUDA(cudaMemcpyAsync(t4, d_total, sizeof(t4), cudaMemcpyDeviceToHost, st));
+        GCOO_CUDA(launch_row_scan_max(h->row_ptr.ptr, h->m, cpg, h->group_index(), h->nnz_per_group(), d_total,
+                                      h->scratch.ptr, h->status.ptr, st));
+        // placed on the device before the one readback (the kernel checks the fit itself)
+        const int64_t packed_cap = static_cast<int64_t>(h->packed.count);
+        GCOO_CUDA(launch_place(h->dA, h->m, h->k, cpg, slot, h->stage.ptr, h->tile_tot.ptr, h->over_list.ptr,
+                               over_count, h->tile_cnt.ptr, h->group_index(), h->row_ptr.ptr, h->vals.ptr, h->rc.ptr,
+                               h->packed.ptr, d_total, cap, packed_cap, st));
+        if (!h->readback && cudaMallocHost(&h->readback, 4 * sizeof(int64_t)) != cudaSuccess) {
+            h->readback = nullptr;
+            return fail(GCOO_ERROR_ALLOC, "page-locked allocation of the readback words failed");
+        }
+        int64_t *t3 = h->readback;
+        GCOO_CUDA(cudaMemcpyAsync(t3, d_total, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
         GCOO_CUDA(cudaStreamSynchronize(st));
-        const int64_t total = t4[0];
-        if (total > 0x7fffffffLL)
+        const int64_t total = t3[0];
+        if (t3[3] == 0 && (total < 0 || total > 0x7fffffffLL))
             return fail(GCOO_ERROR_FORMAT, "nnz = " + std::to_string(total) + " exceeds the int32 GCOO format");
-        if (t4[3] == 0 && total >= 0 && total <= cap) {
-            if (!h->packed.ensure(static_cast<size_t>(total) + 2))
-                return fail(GCOO_ERROR_ALLOC, "device allocation of the packed entries failed");
-            // rows and cols live in one block, as in the reference (src/ShGCOOSpDM.cu:95-97)
-            GCOO_CUDA(cudaMemcpyAsync(h->rc.ptr + total, h->cols_tmp.ptr, static_cast<size_t>(total) * sizeof(int32_t),
-                                      cudaMemcpyDeviceToDevice, st));
-            GCOO_CUDA(launch_pack(h->vals.ptr, h->rc.ptr, h->cols_tmp.ptr, h->group_index(), h->nnz_per_group(),
-                                  h->row_ptr.ptr, h->m, cpg, h->packed.ptr, st));
-            h->max_row_nnz = t4[1];
-            h->distinct_cols = t4[2];
+        if (t3[3] == 0 && total <= cap && total + 2 <= packed_cap) {
+            h->max_row_nnz = t3[1];
+            h->distinct_cols = t3[2];
             h->nnz = total;
             h->built = true;
             if (h->tc)
@@ -309,7 +310,7 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
             h->left = nullptr;
             return GCOO_SUCCESS;
         }
-        GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, 3 * sizeof(int64_t), st));
+        GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, 7 * sizeof(int64_t), st));
     }
     if (tiled) {
         if (!h->tile_cnt.ensure(static_cast<size_t>(h->m * conv_segments(h->k))))
@@ -320,9 +321,8 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
     } else {
         GCOO_CUDA(launch_row_count(h->dA, h->m, h->k, h->row_ptr.ptr, st));
     }
-    GCOO_CUDA(launch_row_scan(h->row_ptr.ptr, h->m, h->p.rows_per_group, h->group_index(), h->nnz_per_group(),
-                              d_total, h->scratch.ptr, h->status.ptr, st));
-    GCOO_CUDA(launch_row_max(h->row_ptr.ptr, h->m, d_total + 1, st));
+    GCOO_CUDA(launch_row_scan_max(h->row_ptr.ptr, h->m, h->p.rows_per_group, h->group_index(), h->nnz_per_group(),
+                                  d_total, h->scratch.ptr, h->status.ptr, st));
     int64_t tot2[3] = {0, 0, 0};
     GCOO_CUDA(cudaMemcpyAsync(tot2, d_total, sizeof(tot2), cudaMemcpyDeviceToHost, st));
     GCOO_CUDA(cudaStreamSynchronize(st));
@@ -334,8 +334,7 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
     const size_t nnz = static_cast<size_t>(total);
     // a little room beyond nnz lets later builds of a similar matrix take the one-pass path
     const size_t room = tiled ? nnz + nnz / 16 + 1024 : nnz;
-    if (!h->vals.ensure(room) || !h->rc.ensure(2 * room) || !h->packed.ensure(nnz + 2) ||
-        (tiled && !h->cols_tmp.ensure(room)))
+    if (!h->vals.ensure(room) || !h->rc.ensure(2 * room) || !h->packed.ensure(room + 2))
         return fail(GCOO_ERROR_ALLOC, "device allocation of the GCOO entry arrays failed");
     // rows and cols live in one block, as in the reference (src/ShGCOOSpDM.cu:95-97)
     int32_t *rows = h->rc.ptr;

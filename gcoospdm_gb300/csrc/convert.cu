@@ -171,6 +171,100 @@ scan_down_kernel(int32_t *__restrict__ data, int64_t m, const int64_t *__restric
     }
 }
 
+// The whole row scan of a matrix of up to kSmallScanRows rows in one CTA:
+// row counts -> row_ptr (in place, row_ptr[m] = total), the total and the
+// longest row into d_total[0] / d_total[1], and the group arrays when given.
+// Same results as scan_reduce / scan_top / scan_down + group_arrays +
+// row_max, in one launch instead of five.
+constexpr int kSmallScanItems = 8;
+constexpr int64_t kSmallScanRows = 131072;
+
+__global__ void __launch_bounds__(kTopThreads)
+scan_small_kernel(int32_t *__restrict__ data, int64_t m, int32_t cpg, int32_t *__restrict__ group_index,
+                  int32_t *__restrict__ nnz_per_group, int64_t *__restrict__ d_total, uint32_t *__restrict__ status)
+{
+    __shared__ int64_t s_warp[32];
+    __shared__ int s_max[32];
+    constexpr int64_t kChunk = static_cast<int64_t>(kTopThreads) * kSmallScanItems;
+    int64_t carry = 0;
+    int mx = 0;
+    for (int64_t c0 = 0; c0 < m; c0 += kChunk) {
+        const int64_t base = c0 + static_cast<int64_t>(threadIdx.x) * kSmallScanItems;
+        int32_t v[kSmallScanItems];
+        int64_t sum = 0;
+#pragma unroll
+        for (int i = 0; i < kSmallScanItems; ++i) {
+            v[i] = base + i < m ? data[base + i] : 0;
+            sum += v[i];
+            mx = v[i] > mx ? v[i] : mx;
+        }
+        int64_t total;
+        int64_t run = carry + block_exclusive_scan<kTopThreads>(sum, s_warp, &total);
+        // whole groups inside the thread's rows (rows_per_group dividing the item count): their
+        // arrays straight from the registers
+        const bool own_groups = group_index && kSmallScanItems % cpg == 0;
+        int32_t gsum = 0;
+        int64_t gstart = run;
+#pragma unroll
+        for (int i = 0; i < kSmallScanItems; ++i) {
+            if (base + i < m)
+                data[base + i] = static_cast<int32_t>(run);
+            run += v[i];
+            gsum += v[i];
+            if (own_groups && (i + 1) % cpg == 0) {
+                const int64_t r0 = base + i + 1 - cpg;
+                if (r0 < m) {
+                    group_index[r0 / cpg] = static_cast<int32_t>(gstart);
+                    nnz_per_group[r0 / cpg] = gsum;
+                }
+                gsum = 0;
+                gstart = run;
+            }
+        }
+        carry += total;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        const int y = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = y > mx ? y : mx;
+    }
+    if ((threadIdx.x & 31) == 0)
+        s_max[threadIdx.x >> 5] = mx;
+    __syncthreads(); // also orders the row_ptr writes above before the group reads below
+    if (threadIdx.x == 0) {
+        int best = 0;
+        for (int w = 0; w < kTopThreads / 32; ++w)
+            best = s_max[w] > best ? s_max[w] : best;
+        d_total[0] = carry;
+        d_total[1] = best;
+        data[m] = static_cast<int32_t>(carry);
+        if (carry > 0x7fffffffLL && status)
+            atomicOr(status, kStatusOverflow);
+    }
+    if (!group_index)
+        return;
+    const int64_t ng = (m + cpg - 1) / cpg;
+    if (kSmallScanItems % cpg == 0) {
+        if (threadIdx.x == 0) {
+            group_index[ng] = static_cast<int32_t>(carry);
+            nnz_per_group[ng] = 0; // the reference memsets nGroup+1 entries
+        }
+        return;
+    }
+    __syncthreads();
+    for (int64_t g = threadIdx.x; g <= ng; g += kTopThreads) {
+        if (g == ng) {
+            group_index[ng] = data[m];
+            nnz_per_group[ng] = 0; // the reference memsets nGroup+1 entries
+        } else {
+            const int64_t r0 = g * cpg;
+            const int64_t r1 = r0 + cpg < m ? r0 + cpg : m;
+            group_index[g] = data[r0];
+            nnz_per_group[g] = data[r1] - data[r0];
+        }
+    }
+}
+
 __global__ void group_arrays_kernel(const int32_t *__restrict__ row_ptr, int64_t m, int32_t cpg,
                                     int64_t ng, int32_t *__restrict__ group_index,
                                     int32_t *__restrict__ nnz_per_group)
@@ -510,6 +604,21 @@ cudaError_t launch_row_scan(int32_t *data, int64_t m, int32_t cpg, int32_t *grou
         e = cudaGetLastError();
     }
     return e;
+}
+
+cudaError_t launch_row_scan_max(int32_t *data, int64_t m, int32_t cpg, int32_t *group_index,
+                                int32_t *nnz_per_group, int64_t *d_total, int64_t *scratch, uint32_t *status,
+                                cudaStream_t st)
+{
+    if (m > 0 && m <= kSmallScanRows) {
+        scan_small_kernel<<<1, kTopThreads, 0, st>>>(data, m, cpg, group_index, nnz_per_group, d_total, status);
+        count_launches(1);
+        return cudaGetLastError();
+    }
+    cudaError_t e = launch_row_scan(data, m, cpg, group_index, nnz_per_group, d_total, scratch, status, st);
+    if (e != cudaSuccess)
+        return e;
+    return launch_row_max(data, m, d_total + 1, st);
 }
 
 cudaError_t launch_scatter(const float *A, int64_t m, int64_t k, int32_t cpg, const int32_t *group_index,

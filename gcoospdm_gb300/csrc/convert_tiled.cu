@@ -42,12 +42,13 @@ struct SegUnit {
     bool live; // segment starts inside the row
 };
 
+// b: the CTA's tile (group-major: b = g * tiles + t)
 template <int CPG>
-__device__ __forceinline__ SegUnit seg_unit(int64_t m, int64_t k, int64_t tiles)
+__device__ __forceinline__ SegUnit seg_unit(int64_t m, int64_t k, int64_t tiles, int64_t b)
 {
     SegUnit u;
-    const int64_t b = blockIdx.x;
-    u.g = b / tiles;
+    // tiles and b < 2^31 (tiled_convert_ok): 32-bit division
+    u.g = static_cast<int64_t>(static_cast<uint32_t>(b) / static_cast<uint32_t>(tiles));
     const int64_t t = b - u.g * tiles;
     u.s = t * kSegsPerCta + (threadIdx.x >> 5);
     u.r0 = u.g * CPG;
@@ -66,7 +67,7 @@ seg_count_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t tile
                  int32_t *__restrict__ cnt, unsigned long long *__restrict__ distinct)
 {
     __shared__ int s_dist[kSegsPerCta];
-    const SegUnit u = seg_unit<CPG>(m, k, tiles);
+    const SegUnit u = seg_unit<CPG>(m, k, tiles, blockIdx.x);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float4 v[CPG];
 #pragma unroll
@@ -131,15 +132,14 @@ __global__ void seg_prefix_kernel(int32_t *__restrict__ cnt, int64_t m, int64_t 
 // this one. Per-lane counts (0..4) are packed four rows to a word in 8-bit
 // fields so one warp scan per word serves four rows at once.
 template <int CPG>
-// 6 CTAs per SM for up to 4 rows per group: more loads of A in flight
-__global__ void __launch_bounds__(kTileThreads, CPG <= 4 ? 6 : 4)
-seg_scatter_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t tiles, int64_t S,
-                   const int32_t *__restrict__ pref, const int32_t *__restrict__ group_index,
-                   const int32_t *__restrict__ row_ptr, float *__restrict__ vals, int32_t *__restrict__ rows,
-                   int32_t *__restrict__ cols, Entry *__restrict__ packed)
+__device__ __forceinline__ void scatter_segment(const float *__restrict__ A, int64_t k, int64_t S, const SegUnit &u,
+                                                const int32_t *__restrict__ pref,
+                                                const int32_t *__restrict__ group_index,
+                                                const int32_t *__restrict__ row_ptr, float *__restrict__ vals,
+                                                int32_t *__restrict__ rows, int32_t *__restrict__ cols,
+                                                Entry *__restrict__ packed)
 {
     constexpr int NP = (CPG + 3) / 4;
-    const SegUnit u = seg_unit<CPG>(m, k, tiles);
     if (!u.live)
         return;
     const int lane = threadIdx.x & 31;
@@ -228,6 +228,253 @@ seg_scatter_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t ti
     }
 }
 
+template <int CPG>
+// 6 CTAs per SM for up to 4 rows per group: more loads of A in flight
+__global__ void __launch_bounds__(kTileThreads, CPG <= 4 ? 6 : 4)
+seg_scatter_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t tiles, int64_t S,
+                   const int32_t *__restrict__ pref, const int32_t *__restrict__ group_index,
+                   const int32_t *__restrict__ row_ptr, float *__restrict__ vals, int32_t *__restrict__ rows,
+                   int32_t *__restrict__ cols, Entry *__restrict__ packed)
+{
+    scatter_segment<CPG>(A, k, S, seg_unit<CPG>(m, k, tiles, blockIdx.x), pref, group_index, row_ptr, vals, rows,
+                         cols, packed);
+}
+
+// ---- staged rebuild: A read once --------------------------------------------------
+// stage_kernel is seg_count_kernel that also keeps each tile's entries (a
+// tile: CPG rows x 1024 columns, one CTA, brought into shared memory by bulk
+// copies) in a fixed slot of `slot` entries,
+// in the tile's GCOO order (column, then row) and as (col << 3 | row in
+// group, value bits). tile_tot[b] = the tile's entry count, or -1 when it
+// overflowed its slot; an overflowed tile is appended to over_list instead.
+// No CTA waits on another. place_kernel then runs after the segment prefix and
+// the row scan: one warp per staged tile copies its entries to
+//   GCOO:   group_index[g] + sum_r prefix[r][first segment of the tile] + i
+//   packed: row_ptr[r] + prefix[r][first segment] + rank of the entry in row r
+// and blocks past the staged ones rescan A for the overflowed tiles with the
+// two-pass scatter. Same arrays as the two-pass conversion, bit for bit.
+template <int CPG>
+__global__ void __launch_bounds__(kTileThreads, CPG <= 4 ? 8 : 6)
+stage_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t tiles, int64_t S, int32_t *__restrict__ cnt,
+             unsigned long long *__restrict__ distinct, int32_t slot, uint2 *__restrict__ stage,
+             int32_t *__restrict__ tile_tot, int32_t *__restrict__ over_list,
+             unsigned long long *__restrict__ over_count, uint32_t *__restrict__ status)
+{
+    // the tile's rows arrive by bulk copies: no registers held while they are in
+    // flight, so a full complement of CTAs per SM keeps A streaming
+    __shared__ __align__(128) float s_a[CPG][kTileCols];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ __align__(16) int s_wtot[kSegsPerCta];
+    __shared__ int s_dist[kSegsPerCta];
+    __shared__ long long s_g; // the tile's group, computed once
+    const int64_t b = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar, 1);
+        fence_mbar_init();
+        const SegUnit u0 = seg_unit<CPG>(m, k, tiles, b);
+        s_g = u0.g;
+        // k % 4 == 0 and a 16-byte aligned A: every row piece starts on 16 bytes and is a multiple of 16 long
+        const int64_t c0 = (b - u0.g * tiles) * kTileCols;
+        const int64_t w = k - c0 < kTileCols ? k - c0 : kTileCols;
+        const uint32_t bytes = static_cast<uint32_t>(w * static_cast<int64_t>(sizeof(float)));
+        mbar_arrive_expect_tx(&s_bar, bytes * static_cast<uint32_t>(u0.nrows));
+        for (int r = 0; r < u0.nrows; ++r)
+            bulk_g2s(s_a[r], A + (u0.r0 + r) * k + c0, bytes, &s_bar);
+    }
+    __syncthreads();
+    SegUnit u;
+    u.g = s_g;
+    {
+        const int64_t t = b - u.g * tiles;
+        u.s = t * kSegsPerCta + warp;
+        u.r0 = u.g * CPG;
+        u.nrows = static_cast<int>(u.r0 + CPG <= m ? CPG : m - u.r0);
+        u.c = u.s * kSegCols + static_cast<int64_t>(lane) * 4;
+        u.live = u.s * kSegCols < k;
+    }
+    // one warp polls the barrier, the others wait at the CTA barrier (no issue
+    // slots spent); a wait that gives up (it never should) flags the build,
+    // which the host then redoes on the two-pass path, once the copies landed
+    bool waited = true;
+    if (warp == 0)
+        waited = mbar_wait_sleep(&s_bar, 0);
+    if (!__syncthreads_and(waited)) {
+        if (threadIdx.x == 0) {
+            atomicOr(status, kStatusWaitTimeout);
+            mbar_wait(&s_bar, 0);
+        }
+        return;
+    }
+    // the lane's nonzeros as one mask in GCOO order: bit q * CPG + r = (row r, column c + q)
+    const int sc = warp * kSegCols + lane * 4; // the lane's first column inside the tile
+    uint32_t msk = 0;
+    if (u.live && u.c < k) {
+#pragma unroll
+        for (int r = 0; r < CPG; ++r) {
+            if (r < u.nrows) {
+                const float4 x = *reinterpret_cast<const float4 *>(&s_a[r][sc]);
+                msk |= (nzb(x.x) << r) | (nzb(x.y) << (CPG + r)) | (nzb(x.z) << (2 * CPG + r)) |
+                       (nzb(x.w) << (3 * CPG + r));
+            }
+        }
+    }
+    constexpr uint32_t kCol = (CPG == 8) ? 0x01010101u : (CPG == 4) ? 0x1111u : (CPG == 2) ? 0x55u : 0xfu;
+    int wsum = 0, my_cnt = 0;
+#pragma unroll
+    for (int r = 0; r < CPG; ++r) {
+        const int x = static_cast<int>(__reduce_add_sync(0xffffffffu, __popc(msk & (kCol << r))));
+        wsum += x;
+        my_cnt = lane == r ? x : my_cnt;
+    }
+    if (u.live && lane < u.nrows)
+        cnt[(u.r0 + lane) * S + u.s] = my_cnt; // lane r: row r's count
+    if (lane == 0) {
+        s_wtot[warp] = wsum;
+        s_dist[warp] = 0;
+    }
+    if (distinct) {
+        // fold the rows of each column onto its lowest bit: the columns with a nonzero
+        uint32_t f = msk;
+#pragma unroll
+        for (int sh = 1; sh < CPG; sh <<= 1)
+            f |= f >> sh;
+        const int d = static_cast<int>(__reduce_add_sync(0xffffffffu, static_cast<uint32_t>(__popc(f & kCol))));
+        if (lane == 0)
+            s_dist[warp] = d;
+    }
+    // the lane's first entry in the warp's part: exclusive prefix of the lanes'
+    // counts, one ballot per count level (a level rarely past 1 or 2 when sparse)
+    const int mine = __popc(msk);
+    const unsigned lt = (1u << lane) - 1u;
+    int before = 0;
+    for (int j = 0; __any_sync(0xffffffffu, mine > j); ++j)
+        before += __popc(__ballot_sync(0xffffffffu, mine > j) & lt);
+    __syncthreads(); // every warp of the CTA reaches this (no early exit above)
+    int off = 0, T = 0;
+    {
+        static_assert(kSegsPerCta == 8, "two int4 loads read the warp totals");
+        const int4 w0 = *reinterpret_cast<const int4 *>(&s_wtot[0]);
+        const int4 w1 = *reinterpret_cast<const int4 *>(&s_wtot[4]);
+        const int wt[kSegsPerCta] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+        for (int w = 0; w < kSegsPerCta; ++w) {
+            off += w < warp ? wt[w] : 0;
+            T += wt[w];
+        }
+    }
+    const bool fits = T <= slot;
+    if (threadIdx.x == 0) {
+        tile_tot[b] = fits ? T : -1;
+        if (!fits)
+            over_list[atomicAdd(over_count, 1ull)] = static_cast<int32_t>(b);
+        if (distinct) {
+            int dsum = 0;
+#pragma unroll
+            for (int w = 0; w < kSegsPerCta; ++w)
+                dsum += s_dist[w];
+            if (dsum)
+                atomicAdd(distinct, static_cast<unsigned long long>(dsum));
+        }
+    }
+    if (!fits)
+        return;
+    int64_t pos = b * static_cast<int64_t>(slot) + off + before;
+    while (msk) {
+        const int i = __ffs(msk) - 1;
+        msk &= msk - 1u;
+        const int q = i / CPG, r = i % CPG;
+        stage[pos++] = make_uint2((static_cast<uint32_t>(u.c + q) << 3) | static_cast<uint32_t>(r),
+                                  __float_as_uint(s_a[r][sc + q]));
+    }
+}
+
+template <int CPG>
+__global__ void __launch_bounds__(kTileThreads, CPG <= 4 ? 6 : 4)
+place_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t tiles, int64_t S, int64_t units,
+             int32_t slot, const uint2 *__restrict__ stage, const int32_t *__restrict__ tile_tot,
+             const int32_t *__restrict__ over_list, const unsigned long long *__restrict__ over_count,
+             const int32_t *__restrict__ pref, const int32_t *__restrict__ group_index,
+             const int32_t *__restrict__ row_ptr, float *__restrict__ vals, int32_t *__restrict__ rc,
+             Entry *__restrict__ packed, const int64_t *__restrict__ d_total, int64_t cap, int64_t packed_cap,
+             int64_t staged_blocks)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool staged_block = static_cast<int64_t>(blockIdx.x) < staged_blocks;
+    const int64_t b = static_cast<int64_t>(blockIdx.x) * kSegsPerCta + warp;
+    // the tile's count is loaded alongside the totals (one round trip)
+    const int32_t T = staged_block && b < units ? tile_tot[b] : 0;
+    const int64_t total = d_total[0];
+    if (d_total[3] != 0 || total < 0 || total > 0x7fffffffLL || total > cap || total + 2 > packed_cap)
+        return; // staging gave up or the arrays are too small: the host converts again on the two-pass path
+    // from here every position is below total < 2^31: 32-bit offsets
+    int32_t *rows = rc, *cols = rc + total; // the reference's one rows|cols block
+    if (staged_block) {
+        if (T <= 0)
+            return; // empty, or overflowed and placed by the rescan blocks
+        const int64_t g = b / tiles, t = b - g * tiles, r0 = g * CPG, s0 = t * kSegsPerCta;
+        const int nrows = static_cast<int>(r0 + CPG <= m ? CPG : m - r0);
+        // every load the tile needs goes out at once: offsets and up to 4 windows of entries
+        const int32_t my_pre = lane < nrows ? pref[(r0 + lane) * S + s0] : 0;
+        const int32_t my_rp = lane < nrows ? row_ptr[r0 + lane] : 0;
+        const int32_t gi = group_index[g];
+        const uint2 *src = stage + b * static_cast<int64_t>(slot);
+        constexpr int kWin = 4;
+        uint2 e[kWin];
+#pragma unroll
+        for (int j = 0; j < kWin; ++j)
+            e[j] = 32 * j + lane < T ? src[32 * j + lane] : make_uint2(0u, 0u);
+        int32_t gpos = static_cast<int32_t>(gi);
+        int32_t base[CPG];
+#pragma unroll
+        for (int r = 0; r < CPG; ++r) {
+            const int32_t pre = __shfl_sync(0xffffffffu, my_pre, r);
+            gpos += pre;
+            base[r] = __shfl_sync(0xffffffffu, my_rp, r) + pre;
+        }
+        const unsigned lt = (1u << lane) - 1u;
+        for (int w0 = 0; w0 < T; w0 += 32 * kWin) {
+            if (w0 > 0) {
+#pragma unroll
+                for (int j = 0; j < kWin; ++j)
+                    e[j] = w0 + 32 * j + lane < T ? src[w0 + 32 * j + lane] : make_uint2(0u, 0u);
+            }
+#pragma unroll
+            for (int j = 0; j < kWin; ++j) {
+                const int w = w0 + 32 * j;
+                if (w >= T)
+                    break;
+                const bool ok = w + lane < T;
+                const int r = static_cast<int>(e[j].x & 7u);
+                const int32_t col = static_cast<int32_t>(e[j].x >> 3);
+                if (ok) {
+                    vals[gpos + w + lane] = __uint_as_float(e[j].y);
+                    rows[gpos + w + lane] = static_cast<int32_t>(r0 + r);
+                    cols[gpos + w + lane] = col;
+                }
+#pragma unroll
+                for (int rr = 0; rr < CPG; ++rr) {
+                    const unsigned mk = __ballot_sync(0xffffffffu, ok && r == rr);
+                    if (ok && r == rr) {
+                        Entry en;
+                        en.col = col;
+                        en.val = __uint_as_float(e[j].y);
+                        packed[base[rr] + __popc(mk & lt)] = en;
+                    }
+                    base[rr] += __popc(mk);
+                }
+            }
+        }
+        return;
+    }
+    // rescan blocks: one overflowed tile at a time, a warp per segment
+    const int64_t n_over = static_cast<int64_t>(*over_count);
+    const int64_t stride = static_cast<int64_t>(gridDim.x) - staged_blocks;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) - staged_blocks; i < n_over; i += stride)
+        scatter_segment<CPG>(A, k, S, seg_unit<CPG>(m, k, tiles, over_list[i]), pref, group_index, row_ptr, vals,
+                             rows, cols, packed);
+}
+
 } // namespace
 
 int64_t conv_segments(int64_t k) { return (k + kSegCols - 1) / kSegCols; }
@@ -292,6 +539,80 @@ cudaError_t launch_tile_scatter(const float *A, int64_t m, int64_t k, int32_t cp
     default: return cudaErrorInvalidValue;
     }
 #undef GCOO_SEG_SCATTER
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+bool staged_convert_ok(const float *A, int64_t m, int64_t k, int32_t cpg)
+{
+    return tiled_convert_ok(A, m, k, cpg) && k < (static_cast<int64_t>(1) << 28);
+}
+
+int64_t staged_tiles(int64_t m, int64_t k, int32_t cpg) { return ((m + cpg - 1) / cpg) * conv_tiles(k); }
+
+int32_t staged_slot(int64_t last_nnz, int64_t tiles, int32_t cpg)
+{
+    const int64_t avg = tiles > 0 && last_nnz > 0 ? (last_nnz + tiles - 1) / tiles : 0;
+    const int64_t want = 2 * avg + 32;
+    // at most 256 entries per row of the tile: the slots take at most half of A's bytes
+    int32_t slot = 32;
+    while (slot < want && slot < 256 * cpg)
+        slot <<= 1;
+    return slot;
+}
+
+cudaError_t launch_stage(const float *A, int64_t m, int64_t k, int32_t cpg, int32_t slot, int32_t *cnt,
+                         unsigned long long *distinct, uint2 *stage, int32_t *tile_tot, int32_t *over_list,
+                         unsigned long long *over_count, uint32_t *status, cudaStream_t st)
+{
+    const int64_t tiles = conv_tiles(k), S = conv_segments(k);
+    const int64_t units = ((m + cpg - 1) / cpg) * tiles;
+    if (units <= 0)
+        return cudaSuccess;
+    const unsigned grid = static_cast<unsigned>(units);
+#define GCOO_STAGE(C)                                                                                        \
+    stage_kernel<C><<<grid, kTileThreads, 0, st>>>(A, m, k, tiles, S, cnt, distinct, slot, stage, tile_tot, \
+                                                   over_list, over_count, status)
+    switch (cpg) {
+    case 1: GCOO_STAGE(1); break;
+    case 2: GCOO_STAGE(2); break;
+    case 4: GCOO_STAGE(4); break;
+    case 8: GCOO_STAGE(8); break;
+    default: return cudaErrorInvalidValue;
+    }
+#undef GCOO_STAGE
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_place(const float *A, int64_t m, int64_t k, int32_t cpg, int32_t slot, const uint2 *stage,
+                         const int32_t *tile_tot, const int32_t *over_list, const unsigned long long *over_count,
+                         const int32_t *pref, const int32_t *group_index, const int32_t *row_ptr, float *vals,
+                         int32_t *rc, Entry *packed, const int64_t *d_total, int64_t cap, int64_t packed_cap,
+                         cudaStream_t st)
+{
+    const int64_t tiles = conv_tiles(k), S = conv_segments(k);
+    const int64_t units = ((m + cpg - 1) / cpg) * tiles;
+    if (units <= 0)
+        return cudaSuccess;
+    const int64_t staged_blocks = (units + kSegsPerCta - 1) / kSegsPerCta;
+    // rescan blocks: enough to cover the GPU for matrices whose tiles mostly overflow
+    int64_t rescan_blocks = static_cast<int64_t>(device_sms()) * 6;
+    if (rescan_blocks > units)
+        rescan_blocks = units;
+    const unsigned grid = static_cast<unsigned>(staged_blocks + rescan_blocks);
+#define GCOO_PLACE(C)                                                                                            \
+    place_kernel<C><<<grid, kTileThreads, 0, st>>>(A, m, k, tiles, S, units, slot, stage, tile_tot, over_list,  \
+                                                   over_count, pref, group_index, row_ptr, vals, rc, packed,   \
+                                                   d_total, cap, packed_cap, staged_blocks)
+    switch (cpg) {
+    case 1: GCOO_PLACE(1); break;
+    case 2: GCOO_PLACE(2); break;
+    case 4: GCOO_PLACE(4); break;
+    case 8: GCOO_PLACE(8); break;
+    default: return cudaErrorInvalidValue;
+    }
+#undef GCOO_PLACE
     count_launches(1);
     return cudaGetLastError();
 }

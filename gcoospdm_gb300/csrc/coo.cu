@@ -188,9 +188,8 @@ gcoo_status coo_build(gcoo_handle *h, cudaStream_t st)
     // row counts -> row pointers and the group arrays; longest row
     int64_t *d_total = h->scratch.ptr + scan_scratch_elems(h->m);
     GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, sizeof(int64_t), st));
-    GCOO_CUDA(launch_row_scan(h->row_ptr.ptr, h->m, cpg, h->group_index(), h->nnz_per_group(), d_total, h->scratch.ptr,
-                              h->status.ptr, st));
-    GCOO_CUDA(launch_row_max(h->row_ptr.ptr, h->m, d_total + 1, st));
+    GCOO_CUDA(launch_row_scan_max(h->row_ptr.ptr, h->m, cpg, h->group_index(), h->nnz_per_group(), d_total,
+                                  h->scratch.ptr, h->status.ptr, st));
     if (total > 0) {
         size_t tmp_bytes = 0;
         const uint64_t maxkey = (static_cast<uint64_t>(h->ng) * static_cast<uint64_t>(h->k)) * static_cast<uint64_t>(cpg);

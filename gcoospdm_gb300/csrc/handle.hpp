@@ -40,9 +40,10 @@ struct gcoo_handle {
     gcoo::DevBuf<int32_t> rc;        // rows[nnz] | cols[nnz]
     gcoo::DevBuf<gcoo::Entry> packed; // row order, nnz + 2 (16-byte padded)
     gcoo::DevBuf<int32_t> tile_cnt;  // per-(row, column segment) counts of the tiled conversion
-    gcoo::DevBuf<int32_t> cols_tmp;  // one-pass conversion: cols before nnz is known
-    gcoo::DevBuf<unsigned long long> unit_state; // one-pass conversion: look-back words
-    gcoo::DevBuf<unsigned int> ticket;           // one-pass conversion: unit ticket
+    gcoo::DevBuf<uint2> stage;       // staged rebuild: each tile's entries in a fixed slot
+    gcoo::DevBuf<int32_t> tile_tot;  // staged rebuild: entries per tile, -1 when it overflowed
+    gcoo::DevBuf<int32_t> over_list; // staged rebuild: the overflowed tiles
+    int64_t *readback = nullptr;     // page-locked: the staged build's readback
     gcoo::DevBuf<int64_t> scratch;   // scan block sums (+1) and the total
     gcoo::DevBuf<uint32_t> status;   // device status word
     gcoo::DevBuf<double> norm;       // error-norm accumulators
@@ -56,6 +57,8 @@ struct gcoo_handle {
 
     ~gcoo_handle()
     {
+        if (readback)
+            cudaFreeHost(readback);
         gcoo::destroy_tc_plan(tc);
         gcoo::destroy_lowp_work(lowp);
         gcoo::destroy_left_plan(left);

@@ -102,6 +102,11 @@ size_t scan_scratch_elems(int64_t m);
 cudaError_t launch_row_scan(int32_t *row_counts_then_ptr, int64_t m, int32_t rows_per_group,
                             int32_t *group_index, int32_t *nnz_per_group, int64_t *d_total,
                             int64_t *scratch, uint32_t *status, cudaStream_t st);
+// launch_row_scan followed by the longest row into d_total[1] (zeroed by the
+// caller): one single-CTA kernel for up to 131072 rows, else the two launches.
+cudaError_t launch_row_scan_max(int32_t *row_counts_then_ptr, int64_t m, int32_t rows_per_group,
+                                int32_t *group_index, int32_t *nnz_per_group, int64_t *d_total,
+                                int64_t *scratch, uint32_t *status, cudaStream_t st);
 // Group arrays only (count entry point without row pointers): from row counts.
 cudaError_t launch_scatter(const float *A, int64_t m, int64_t k, int32_t rows_per_group,
                            const int32_t *group_index, const int32_t *row_ptr, float *vals,
@@ -123,24 +128,30 @@ cudaError_t launch_tile_scatter(const float *A, int64_t m, int64_t k, int32_t cp
                                 const int32_t *group_index, const int32_t *row_ptr, float *vals,
                                 int32_t *rows, int32_t *cols, Entry *packed, cudaStream_t st);
 
-// ---- one-pass conversion (convert_onepass.cu) ----------------------------------------
-// Same arrays as the tiled conversion from one read of A: GCOO arrays written
-// up to `cap` entries (cols into their own array), group_index, the segment
-// counts and the total (d_total[0]); *status gets kStatusOverflow when the
-// arrays were too small and kStatusWaitTimeout when a look-back gave up.
-bool onepass_convert_ok(const float *A, int64_t m, int64_t k, int32_t cpg);
-int64_t onepass_units(int64_t m, int64_t k, int32_t cpg);
-cudaError_t launch_onepass(const float *A, int64_t m, int64_t k, int32_t cpg, int32_t *cnt,
-                           unsigned long long *distinct, unsigned long long *state, unsigned int *ticket,
-                           float *vals, int32_t *rows, int32_t *cols, int64_t cap, int32_t *group_index,
-                           int64_t *d_total, uint32_t *status, cudaStream_t st);
-// Row-ordered packed entries from the GCOO arrays and row pointers, and
-// nnz_per_group from group_index (when not null).
-cudaError_t launch_pack(const float *vals, const int32_t *rows, const int32_t *cols, int32_t *group_index,
-                        int32_t *nnz_per_group, const int32_t *row_ptr, int64_t m, int32_t cpg, Entry *packed,
-                        cudaStream_t st);
+// ---- staged rebuild conversion (convert_tiled.cu): A read once -----------------------
+// Needs tiled_convert_ok and k < 2^28 (a staged entry keeps col << 3 | row in group).
+bool staged_convert_ok(const float *A, int64_t m, int64_t k, int32_t cpg);
+int64_t staged_tiles(int64_t m, int64_t k, int32_t cpg); // CPG rows x 1024 columns each
+// Entries kept per tile: a power of two >= 2 x the mean of the last build + 32.
+int32_t staged_slot(int64_t last_nnz, int64_t tiles, int32_t cpg);
+// Segment counts (as launch_tile_count, distinct included), tile_tot[t] (-1
+// for a tile that overflowed its slot, listed in over_list[0..*over_count));
+// *status gets kStatusWaitTimeout if a bulk copy wait gave up.
+cudaError_t launch_stage(const float *A, int64_t m, int64_t k, int32_t cpg, int32_t slot, int32_t *cnt,
+                         unsigned long long *distinct, uint2 *stage, int32_t *tile_tot, int32_t *over_list,
+                         unsigned long long *over_count, uint32_t *status, cudaStream_t st);
+// After launch_tile_prefix and launch_row_scan: the GCOO arrays (vals, rc =
+// rows | cols at rc + total) and the packed row order, total = d_total[0] read
+// on the device; writes nothing unless the stage status (d_total[3]) is 0,
+// total <= cap and total + 2 <= packed_cap.
+cudaError_t launch_place(const float *A, int64_t m, int64_t k, int32_t cpg, int32_t slot, const uint2 *stage,
+                         const int32_t *tile_tot, const int32_t *over_list, const unsigned long long *over_count,
+                         const int32_t *pref, const int32_t *group_index, const int32_t *row_ptr, float *vals,
+                         int32_t *rc, Entry *packed, const int64_t *d_total, int64_t cap, int64_t packed_cap,
+                         cudaStream_t st);
 
 // ---- FP32 multiply (spdm_fp32.cu) ------------------------------------------------------
+int device_sms(); // SMs of the current device (152 on a GB300)
 struct LaunchShape {
     int vec;       // columns per thread (1, 2, 4)
     int warps;     // warps per CTA
@@ -253,6 +264,34 @@ __device__ __forceinline__ bool mbar_wait_ns(uint64_t *bar, uint32_t parity, uin
         if (it == 0)
             t0 = now;
         else if (now - t0 > limit_ns)
+            return false;
+    }
+    return false;
+}
+
+// mbar_wait for a waiter with nothing else to do: each poll lets the hardware
+// suspend the thread for up to 20 us (it resumes as soon as the phase
+// completes), so a waiting warp takes almost no issue slots from the warps
+// that compute. Same limits and result as mbar_wait.
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity)
+{
+    const uint32_t addr = smem_u32(bar);
+    constexpr uint32_t kSuspendNs = 20000;
+    uint64_t t0 = 0;
+    for (uint32_t it = 0; it < kWaitLimit; ++it) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done)
+                     : "r"(addr), "r"(parity), "r"(kSuspendNs)
+                     : "memory");
+        if (done)
+            return true;
+        const uint64_t now = global_ns();
+        if (it == 0)
+            t0 = now;
+        else if (now - t0 > kWaitNs)
             return false;
     }
     return false;

@@ -131,8 +131,7 @@ gcoo_status left_prepare(gcoo_handle *h, LeftPlan *&plan, int64_t p, cudaStream_
         }
         int64_t *d_tot = sc.ptr + scn;
         GCOO_CUDA(cudaMemsetAsync(d_tot + 1, 0, sizeof(int64_t), st));
-        GCOO_CUDA(launch_row_scan(L.col_ptr.ptr, h->k, 1, nullptr, nullptr, d_tot, sc.ptr, nullptr, st));
-        GCOO_CUDA(launch_row_max(L.col_ptr.ptr, h->k, d_tot + 1, st));
+        GCOO_CUDA(launch_row_scan_max(L.col_ptr.ptr, h->k, 1, nullptr, nullptr, d_tot, sc.ptr, nullptr, st));
         int64_t t2[2] = {0, 0};
         GCOO_CUDA(cudaMemcpyAsync(t2, d_tot, sizeof(t2), cudaMemcpyDeviceToHost, st));
         GCOO_CUDA(cudaStreamSynchronize(st)); // temporaries are released on return

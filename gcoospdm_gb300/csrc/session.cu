@@ -238,8 +238,8 @@ gcoo_status gcoo_session_multiply(gcoo_session *s, const float *hA, int64_t m, i
         } else {
             GCOO_CUDA(launch_row_count(Ap, rows, k, L.row_ptr.ptr, L.s));
         }
-        GCOO_CUDA(launch_row_scan(L.row_ptr.ptr, rows, cpg, nullptr, nullptr, d_total, L.scratch.ptr, s->status.ptr,
-                                  L.s));
+        GCOO_CUDA(launch_row_scan_max(L.row_ptr.ptr, rows, cpg, nullptr, nullptr, d_total, L.scratch.ptr,
+                                      s->status.ptr, L.s));
         if (tiled)
             GCOO_CUDA(launch_tile_scatter(Ap, rows, k, cpg, L.tile_cnt.ptr, nullptr, L.row_ptr.ptr, nullptr, nullptr,
                                           nullptr, L.packed.ptr, L.s));

@@ -315,6 +315,8 @@ spdm_view_kernel(const float *__restrict__ vals, const int32_t *__restrict__ row
     }
 }
 
+} // namespace
+
 int device_sms()
 {
     static int sms = 0;
@@ -326,8 +328,6 @@ int device_sms()
     }
     return sms;
 }
-
-} // namespace
 
 LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, int64_t max_row,
                        uintptr_t b_addr, uintptr_t c_addr)

@@ -120,9 +120,9 @@ def test_rebuild_after_change(native, oracle_mod, torch):
 
 @pytest.mark.parametrize("name", GOLDEN)
 def test_one_pass_rebuild_matches_reference(native, oracle_mod, torch, manifest, name):
-    """A second build of the same handle reads A once (decoupled look-back
-    over column tiles, the row order derived from the GCOO arrays): the same
-    arrays as the fixtures, and the same FP32 product."""
+    """A second build of the same handle reads A once (each tile's entries
+    staged in a slot, then placed after the scans): the same arrays as the
+    fixtures, and the same FP32 product."""
     entry = manifest["cases"][name]
     A, B = golden_inputs(entry, name)
     h = native.GcooHandle(dev(torch, A), rows_per_group=entry["cpg"]).build()
@@ -157,7 +157,7 @@ def test_one_pass_rebuild_matches_oracle(native, oracle_mod, torch, m, k, p, cpg
 
 
 def test_one_pass_capacity_fallback_and_shrink(native, oracle_mod, torch):
-    """Rebuild after A got denser than the arrays allow (the one-pass attempt
+    """Rebuild after A got denser than the arrays allow (the staged attempt
     falls back to the two-pass path) and after it got sparser (one pass)."""
     from gcoospdm_gb300 import datagen as dg
     A1 = dg.bernoulli_dense(51, 2000, 1024, 0.01)
@@ -175,6 +175,35 @@ def test_one_pass_capacity_fallback_and_shrink(native, oracle_mod, torch):
         for f in FIELDS:
             np.testing.assert_array_equal(host(a[f]), getattr(g, f), err_msg=f)
         assert h.device_status() == 0
+
+
+def test_staged_rebuild_overflowed_tiles(native, oracle_mod, torch):
+    """Rebuild where a few tiles (4 rows x 1024 columns) hold far more entries
+    than their staging slot (sized from the last build): those tiles are
+    rescanned from A, the others placed from their slots. Includes the last,
+    partial group and the last, partial tile."""
+    from gcoospdm_gb300 import datagen as dg
+    m, k = 1030, 3000
+    dA = dev(torch, dg.bernoulli_dense(61, m, k, 0.02))
+    h = native.GcooHandle(dA).build()
+    A2 = dg.bernoulli_dense(62, m, k, 0.004)
+    rng = np.random.default_rng(63)
+    for r0, r1, c0, c1 in ((0, 4, 0, 1024), (500, 504, 1024, 2048), (1028, 1030, 2048, 3000), (8, 12, 40, 1000)):
+        blk = rng.uniform(-1.0, 1.0, size=(r1 - r0, c1 - c0)).astype(np.float32)
+        A2[r0:r1, c0:c1] = np.where(blk == 0.0, np.float32(0.5), blk)
+    dA.copy_(dev(torch, A2))
+    for _ in range(2):
+        h.build()
+        g = oracle_mod.convert(A2)
+        a = h.export()
+        assert a["nnz"] == g.nnz
+        for f in FIELDS:
+            np.testing.assert_array_equal(host(a[f]), getattr(g, f), err_msg=f)
+        assert h.device_status() == 0
+        assert h.check_arrays() == 0
+    B = dg.dense_pm1(64, 1, k, 40)
+    ref = oracle_mod.spdm(g, B)
+    assert np.array_equal(h.spdm(dev(torch, B)).cpu().numpy().view(np.uint32), ref.view(np.uint32))
 
 
 def test_full_size_properties_8192(native, torch):
