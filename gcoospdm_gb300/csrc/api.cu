@@ -141,6 +141,24 @@ gcoo_status spdm_fp32(gcoo_handle *h, const float *dB, int64_t n, float *dC, cud
             p.depth = t.depth;
         }
     }
+    // a skewed matrix (tuned or overridden shapes aside): its long rows go to
+    // their own kernel, the short rest to a kernel without staging
+    if (!override_params && h->n_long > 0 && h->side && long_rows_ok(n, dB)) {
+        // the two kernels write disjoint rows of C: the long rows run on the
+        // side stream, forked from and joined back into the caller's stream
+        GCOO_CUDA(cudaEventRecord(h->ev_fork, st));
+        GCOO_CUDA(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
+        cudaError_t e = launch_spdm_long(h->packed.ptr, h->row_ptr.ptr, h->long_rows.ptr, h->n_long, dB, n, dC,
+                                         h->side);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "spdm_long_kernel launch");
+        e = launch_spdm_short(h->packed.ptr, h->row_ptr.ptr, h->m, dB, n, dC, long_row_min(), st);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "spdm_short_kernel launch");
+        GCOO_CUDA(cudaEventRecord(h->ev_join, h->side));
+        GCOO_CUDA(cudaStreamWaitEvent(st, h->ev_join, 0));
+        return GCOO_SUCCESS;
+    }
     const LaunchShape s = pick_shape(p, h->m, n, h->nnz, h->max_row_nnz, reinterpret_cast<uintptr_t>(dB),
                                      reinterpret_cast<uintptr_t>(dC));
     cudaError_t e = launch_spdm_fp32(h->packed.ptr, h->row_ptr.ptr, h->m, dB, n, dC, s, h->status.ptr, st);
@@ -237,6 +255,45 @@ gcoo_status gcoo_create(gcoo_handle **out, const float *dA, int64_t m, int64_t k
     return GCOO_SUCCESS;
 }
 
+namespace {
+
+// The end of every successful build: plans derived from the old arrays go,
+// and for a skewed matrix the list of its long rows (multiplied by their own
+// kernel) is collected, one readback of its length.
+gcoo_status finish_build(gcoo_handle *h, cudaStream_t st)
+{
+    if (h->tc)
+        destroy_tc_plan(h->tc);
+    h->tc = nullptr;
+    destroy_left_plan(h->left);
+    h->left = nullptr;
+    h->n_long = 0;
+    if (row_lengths_skewed(h->m, h->nnz, h->max_row_nnz) && h->packed.count >= static_cast<size_t>(h->nnz) + 2) {
+        const int64_t cap = h->nnz / long_row_min() + 1;
+        if (!h->long_rows.ensure(static_cast<size_t>(cap)) || !h->long_count.ensure(1))
+            return fail(GCOO_ERROR_ALLOC, "device allocation of the long-row list failed");
+        unsigned long long *d_cnt = h->long_count.ptr;
+        GCOO_CUDA(cudaMemsetAsync(d_cnt, 0, sizeof(*d_cnt), st));
+        GCOO_CUDA(launch_collect_long(h->row_ptr.ptr, h->m, h->long_rows.ptr, cap, d_cnt, st));
+        if (!h->readback && cudaMallocHost(&h->readback, 4 * sizeof(int64_t)) != cudaSuccess) {
+            h->readback = nullptr;
+            return fail(GCOO_ERROR_ALLOC, "page-locked allocation of the readback words failed");
+        }
+        GCOO_CUDA(cudaMemcpyAsync(h->readback, d_cnt, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        GCOO_CUDA(cudaStreamSynchronize(st));
+        h->n_long = std::min<int64_t>(h->readback[0], cap);
+        if (h->n_long > 0 && !h->side) {
+            GCOO_CUDA(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+            GCOO_CUDA(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+            GCOO_CUDA(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+        }
+    }
+    h->built = true;
+    return GCOO_SUCCESS;
+}
+
+} // namespace
+
 gcoo_status gcoo_build(gcoo_handle *h, void *stream)
 {
     NvtxRange nvtx("gcoo_build");
@@ -248,12 +305,7 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
         gcoo_status s = coo_build(h, st);
         if (s != GCOO_SUCCESS)
             return s;
-        h->built = true;
-        destroy_tc_plan(h->tc);
-        h->tc = nullptr;
-        destroy_left_plan(h->left);
-        h->left = nullptr;
-        return GCOO_SUCCESS;
+        return finish_build(h, st);
     }
     const size_t sc = scan_scratch_elems(h->m);
     if (!h->row_ptr.ensure(static_cast<size_t>(h->m) + 1) || !h->groups.ensure(2 * static_cast<size_t>(h->ng + 1)) ||
@@ -302,13 +354,7 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
             h->max_row_nnz = t3[1];
             h->distinct_cols = t3[2];
             h->nnz = total;
-            h->built = true;
-            if (h->tc)
-                destroy_tc_plan(h->tc);
-            h->tc = nullptr;
-            destroy_left_plan(h->left);
-            h->left = nullptr;
-            return GCOO_SUCCESS;
+            return finish_build(h, st);
         }
         GCOO_CUDA(cudaMemsetAsync(d_total + 1, 0, 7 * sizeof(int64_t), st));
     }
@@ -346,13 +392,7 @@ gcoo_status gcoo_build(gcoo_handle *h, void *stream)
         GCOO_CUDA(launch_scatter(h->dA, h->m, h->k, cpg, h->group_index(), h->row_ptr.ptr, h->vals.ptr, rows,
                                  cols, h->packed.ptr, st));
     h->nnz = total;
-    h->built = true;
-    if (h->tc)
-        destroy_tc_plan(h->tc);
-    h->tc = nullptr;
-    destroy_left_plan(h->left);
-    h->left = nullptr;
-    return GCOO_SUCCESS;
+    return finish_build(h, st);
 }
 
 gcoo_status gcoo_spdm_left(gcoo_handle *h, const float *dD, int64_t p, float *dC, void *stream)

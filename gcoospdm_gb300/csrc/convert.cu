@@ -177,7 +177,7 @@ scan_down_kernel(int32_t *__restrict__ data, int64_t m, const int64_t *__restric
 // Same results as scan_reduce / scan_top / scan_down + group_arrays +
 // row_max, in one launch instead of five.
 constexpr int kSmallScanItems = 8;
-constexpr int64_t kSmallScanRows = 131072;
+constexpr int64_t kSmallScanRows = 16384; // two chunks; the three-kernel scan is faster beyond
 
 __global__ void __launch_bounds__(kTopThreads)
 scan_small_kernel(int32_t *__restrict__ data, int64_t m, int32_t cpg, int32_t *__restrict__ group_index,

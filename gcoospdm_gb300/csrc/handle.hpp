@@ -44,6 +44,12 @@ struct gcoo_handle {
     gcoo::DevBuf<int32_t> tile_tot;  // staged rebuild: entries per tile, -1 when it overflowed
     gcoo::DevBuf<int32_t> over_list; // staged rebuild: the overflowed tiles
     int64_t *readback = nullptr;     // page-locked: the staged build's readback
+    gcoo::DevBuf<int32_t> long_rows; // skewed matrices: rows multiplied by the long-row kernel
+    gcoo::DevBuf<unsigned long long> long_count;
+    int64_t n_long = 0;
+    // the long-row kernel runs beside the short-row one: a side stream joined by events
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     gcoo::DevBuf<int64_t> scratch;   // scan block sums (+1) and the total
     gcoo::DevBuf<uint32_t> status;   // device status word
     gcoo::DevBuf<double> norm;       // error-norm accumulators
@@ -59,6 +65,12 @@ struct gcoo_handle {
     {
         if (readback)
             cudaFreeHost(readback);
+        if (ev_fork)
+            cudaEventDestroy(ev_fork);
+        if (ev_join)
+            cudaEventDestroy(ev_join);
+        if (side)
+            cudaStreamDestroy(side);
         gcoo::destroy_tc_plan(tc);
         gcoo::destroy_lowp_work(lowp);
         gcoo::destroy_left_plan(left);

@@ -103,7 +103,7 @@ cudaError_t launch_row_scan(int32_t *row_counts_then_ptr, int64_t m, int32_t row
                             int32_t *group_index, int32_t *nnz_per_group, int64_t *d_total,
                             int64_t *scratch, uint32_t *status, cudaStream_t st);
 // launch_row_scan followed by the longest row into d_total[1] (zeroed by the
-// caller): one single-CTA kernel for up to 131072 rows, else the two launches.
+// caller): one single-CTA kernel for up to 16384 rows, else the two launches.
 cudaError_t launch_row_scan_max(int32_t *row_counts_then_ptr, int64_t m, int32_t rows_per_group,
                                 int32_t *group_index, int32_t *nnz_per_group, int64_t *d_total,
                                 int64_t *scratch, uint32_t *status, cudaStream_t st);
@@ -160,11 +160,27 @@ struct LaunchShape {
     int rows;      // rows per CTA
     int col_iters = 1; // column tiles each warp walks with one staging of its group's entries
 };
+// Heavy-tailed row lengths: the longest row at least 256 entries and above 8x the mean.
+bool row_lengths_skewed(int64_t m, int64_t nnz, int64_t max_row);
 LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, int64_t max_row,
                        uintptr_t b_addr, uintptr_t c_addr);
 cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_t m, const float *B,
                              int64_t n, float *C, const LaunchShape &s, uint32_t *status,
                              cudaStream_t st);
+// The rows shorter than long_min, one warp per (row, column tile), nothing
+// staged (skewed matrices, whose long rows go to launch_spdm_long).
+cudaError_t launch_spdm_short(const Entry *packed, const int32_t *row_ptr, int64_t m, const float *B, int64_t n,
+                              float *C, int32_t long_min, cudaStream_t st);
+// ---- long rows of skewed matrices (spdm_long.cu) -----------------------------------------
+int32_t long_row_min(); // 256 entries
+// n % 4 == 0 and a 16-byte aligned B (16-byte copies of B row pieces)
+bool long_rows_ok(int64_t n, const float *B);
+// list[0..min(*count, cap)) = the rows of at least long_row_min() entries (any order)
+cudaError_t launch_collect_long(const int32_t *row_ptr, int64_t m, int32_t *list, int64_t cap,
+                                unsigned long long *count, cudaStream_t st);
+// C rows of the listed rows, the same fmaf chains as launch_spdm_fp32
+cudaError_t launch_spdm_long(const Entry *packed, const int32_t *row_ptr, const int32_t *list, int64_t n_long,
+                             const float *B, int64_t n, float *C, cudaStream_t st);
 // FP32 multiply in GCOO order (spdm_fp32_group.cu): one B load per column
 // shared by a group's rows; groups of 4 rows; vec 1, 2, 4 or 8.
 bool group_order_ok(int32_t rows_per_group);

@@ -282,6 +282,68 @@ spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ r
     }
 }
 
+// The short rows of a skewed matrix (its long rows go to spdm_long.cu): one
+// warp per (row, 32*V-column tile), nothing staged and no CTA barrier -- a
+// row of a dozen entries is all latency, and the staging round trip and the
+// group's barrier would double it. Lane i loads entry i of each 32-entry
+// window; the B rows of eight entries at a time are loaded with their columns
+// shuffled from the owning lanes; each column's fmaf chain runs over the row's
+// entries in column order from 0.0f, as in every other FP32 kernel.
+template <int V>
+__global__ void __launch_bounds__(256, 4)
+spdm_short_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ row_ptr, int64_t m,
+                  const float *__restrict__ B, int64_t n, float *__restrict__ C, int32_t tiles, int32_t long_min)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t gw = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t row = gw / tiles;
+    if (row >= m)
+        return;
+    const int t = static_cast<int>(gw - row * tiles);
+    const int64_t j = static_cast<int64_t>(t) * (32 * V) + static_cast<int64_t>(lane) * V;
+    const int32_t rs = row_ptr[row];
+    const int cnt = row_ptr[row + 1] - rs;
+    if (long_min > 0 && cnt >= long_min)
+        return; // the long-row kernel writes this row (warp-uniform)
+    const bool has_col = j < n;
+    const float *Bj = B + (has_col ? j : 0);
+    float acc[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+        acc[v] = 0.0f;
+    for (int w0 = 0; w0 < cnt; w0 += 32) {
+        const int nw = cnt - w0 < 32 ? cnt - w0 : 32;
+        Entry my;
+        my.col = 0;
+        my.val = 0.0f;
+        if (lane < nw)
+            my = packed[rs + w0 + lane];
+        for (int u0 = 0; u0 < nw; u0 += 8) {
+            float a[8], b[8][V];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int col = __shfl_sync(0xffffffffu, my.col, (u0 + u) & 31);
+                a[u] = __shfl_sync(0xffffffffu, my.val, (u0 + u) & 31);
+                if (u0 + u < nw && has_col) {
+                    Vec<V>::load(Bj + static_cast<int64_t>(col) * n, b[u]);
+                } else {
+#pragma unroll
+                    for (int v = 0; v < V; ++v)
+                        b[u][v] = 0.0f;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (u0 + u < nw)
+#pragma unroll
+                    for (int v = 0; v < V; ++v)
+                        acc[v] = fmaf(a[u], b[u][v], acc[v]);
+        }
+    }
+    if (has_col)
+        Vec<V>::store(C + row * n + j, acc);
+}
+
 // Multiply straight from reference-layout arrays (entries of a group in
 // column-then-row order, separate vals/rows/cols): one thread per output
 // column, one shared-memory accumulator per (group row, column) so any
@@ -329,6 +391,12 @@ int device_sms()
     return sms;
 }
 
+bool row_lengths_skewed(int64_t m, int64_t nnz, int64_t max_row)
+{
+    const double mean = m > 0 ? static_cast<double>(nnz) / static_cast<double>(m) : 0.0;
+    return max_row >= 256 && static_cast<double>(max_row) > 8.0 * (mean > 1.0 ? mean : 1.0);
+}
+
 LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, int64_t max_row,
                        uintptr_t b_addr, uintptr_t c_addr)
 {
@@ -338,7 +406,7 @@ LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, 
     // the next batch's B loads in flight, since a long row is one long
     // dependent chain. The per-element fmaf order is the same either way.
     const double mean = m > 0 ? static_cast<double>(nnz) / static_cast<double>(m) : 0.0;
-    const bool skewed = max_row >= 256 && static_cast<double>(max_row) > 8.0 * (mean > 1.0 ? mean : 1.0);
+    const bool skewed = row_lengths_skewed(m, nnz, max_row);
     s.rows = skewed ? 1 : p.rows_per_group;
     int vmax = 4;
     if (n % 4 != 0 || (b_addr & 15) || (c_addr & 15))
@@ -425,6 +493,34 @@ cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_
     }
 #undef GCOO_FP32_VEC
 #undef GCOO_FP32_LAUNCH
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spdm_short(const Entry *packed, const int32_t *row_ptr, int64_t m, const float *B, int64_t n,
+                              float *C, int32_t long_min, cudaStream_t st)
+{
+    if (m <= 0 || n <= 0)
+        return cudaSuccess;
+    const uintptr_t b = reinterpret_cast<uintptr_t>(B), c = reinterpret_cast<uintptr_t>(C);
+    int v = 1;
+    if (n % 4 == 0 && !(b & 15) && !(c & 15))
+        v = 4;
+    else if (n % 2 == 0 && !(b & 7) && !(c & 7))
+        v = 2;
+    const int64_t tiles = (n + 32 * v - 1) / (32 * v);
+    const int64_t warps = m * tiles;
+    const int64_t blocks = (warps + 7) / 8;
+    if (tiles > 0x7fffffffLL || blocks > 0x7fffffffLL)
+        return cudaErrorInvalidConfiguration;
+    const unsigned grid = static_cast<unsigned>(blocks);
+    const int32_t nt = static_cast<int32_t>(tiles);
+    if (v == 4)
+        spdm_short_kernel<4><<<grid, 256, 0, st>>>(packed, row_ptr, m, B, n, C, nt, long_min);
+    else if (v == 2)
+        spdm_short_kernel<2><<<grid, 256, 0, st>>>(packed, row_ptr, m, B, n, C, nt, long_min);
+    else
+        spdm_short_kernel<1><<<grid, 256, 0, st>>>(packed, row_ptr, m, B, n, C, nt, long_min);
     count_launches(1);
     return cudaGetLastError();
 }

@@ -113,6 +113,46 @@ def test_heavy_group_multi_chunk(native, oracle_mod, torch):
     assert same_bits(h.spdm(dev(torch, B)).cpu().numpy(), ref)
 
 
+@pytest.mark.parametrize("n", [256, 200, 98, 36])
+def test_long_rows_of_skewed_matrices(native, oracle_mod, torch, n):
+    """Skewed row lengths: rows of at least 256 entries go to the long-row
+    kernel (a deep shared-memory ring of B row pieces per warp), the others to
+    the row kernel. Rows at the threshold, long rows starting on odd and even
+    entries, lengths that are not multiples of 32, a last column tile cut
+    short; n % 4 != 0 leaves every row to the row kernel. Bit-identical to the
+    oracle either way, also after a staged rebuild and from COO input."""
+    from gcoospdm_gb300 import datagen as dg
+    m, k = 600, 5000
+    A = dg.bernoulli_dense(31, m, k, 0.002)
+    rng = np.random.default_rng(32)
+    for r, length in ((3, 255), (4, 256), (5, 257), (6, 4999), (7, 1000), (8, 1001), (100, 3333), (599, 300)):
+        A[r, :] = 0
+        cols = np.sort(rng.choice(k, size=length, replace=False))
+        v = rng.uniform(-1.0, 1.0, size=length).astype(np.float32)
+        A[r, cols] = np.where(v == 0.0, np.float32(0.5), v)
+    B = dg.dense_pm1(33, 1, k, n)
+    ref = oracle_mod.spdm(oracle_mod.convert(A), B)
+    dA, dB = dev(torch, A), dev(torch, B)
+    h = native.GcooHandle(dA).build()
+    assert same_bits(h.spdm(dB).cpu().numpy(), ref)
+    h.build()
+    assert same_bits(h.spdm(dB).cpu().numpy(), ref)
+    r, c = torch.nonzero(dA, as_tuple=True)
+    hc = native.GcooHandle.from_coo(r.int().contiguous(), c.int().contiguous(), dA[r, c].contiguous(), m, k).build()
+    assert same_bits(hc.spdm(dB).cpu().numpy(), ref)
+    # the long rows run on a side stream forked from the caller's: captured and replayed in a graph
+    Cd = torch.empty(m, n, device="cuda")
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=s):
+        h.spdm(dB, Cd, stream=s)
+    Cd.zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert same_bits(Cd.cpu().numpy(), ref)
+
+
 @pytest.mark.parametrize("n,vec", [(4100, 4), (4102, 2), (4099, 1), (1920, 4)])
 def test_short_rows_walk_several_column_tiles(native, oracle_mod, torch, n, vec):
     """Short rows (about 2.5 entries) over many groups and a wide, ragged n:
