@@ -171,6 +171,10 @@ cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_
 // staged (skewed matrices, whose long rows go to launch_spdm_long).
 cudaError_t launch_spdm_short(const Entry *packed, const int32_t *row_ptr, int64_t m, const float *B, int64_t n,
                               float *C, int32_t long_min, cudaStream_t st);
+// ---- FP8-B scales (spdm_lowp.cu) -----------------------------------------------------------
+// scale[j] = the smallest power of two with absmax(B[:, j]) / scale[j] <= 448;
+// n % 4 == 0, B 16-byte aligned; amax: n words of scratch.
+cudaError_t launch_fp8_scales(const float *B, int64_t k, int64_t n, unsigned *amax, float *scale, cudaStream_t st);
 // ---- long rows of skewed matrices (spdm_long.cu) -----------------------------------------
 int32_t long_row_min(); // 256 entries
 // n % 4 == 0 and a 16-byte aligned B (16-byte copies of B row pieces)

@@ -46,15 +46,27 @@ template <> struct FormTraits<kBF16> { static constexpr int V = 8; using T = uin
 template <> struct FormTraits<kSplit> { static constexpr int V = 4; using T = uint32_t; };
 template <> struct FormTraits<kFP8> { static constexpr int V = 16; using T = uint8_t; };
 
+// acc + a * b with bf16 a and b, one rounding (the mixed-precision FMA of
+// sm_100+): the same result as fmaf on the widened values, since a product of
+// two bf16 values is exact in FP32 -- without widening each B value first.
+__device__ __forceinline__ float fma_bf16(uint16_t a, uint16_t b, float c)
+{
+    float d;
+    asm("fma.rn.f32.bf16 %0, %1, %2, %3;" : "=f"(d) : "h"(a), "h"(b), "f"(c));
+    return d;
+}
+
 template <int F>
 __device__ __forceinline__ void fma_entry(float a, const uint4 &w, float (&acc)[FormTraits<F>::V])
 {
     if constexpr (F == kBF16) {
+        // a is already a bf16 value: its top 16 bits are exact
+        const uint16_t ab = static_cast<uint16_t>(__float_as_uint(a) >> 16);
         const uint32_t x[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-            acc[2 * i] = fmaf(a, bf_lo(x[i]), acc[2 * i]);
-            acc[2 * i + 1] = fmaf(a, bf_hi(x[i]), acc[2 * i + 1]);
+            acc[2 * i] = fma_bf16(ab, static_cast<uint16_t>(x[i] & 0xffffu), acc[2 * i]);
+            acc[2 * i + 1] = fma_bf16(ab, static_cast<uint16_t>(x[i] >> 16), acc[2 * i + 1]);
         }
     } else if constexpr (F == kFP8) {
         const uint32_t x[4] = {w.x, w.y, w.z, w.w};
@@ -249,12 +261,22 @@ __global__ void colmax_kernel(const float *__restrict__ B, int64_t k, int64_t n,
     atomicMax(amax + j + 3, __float_as_uint(m3));
 }
 
+// Per-column scale: the smallest power of two s with absmax / s <= 448 (the
+// largest E4M3 value). A power of two divides exactly, so both engines see
+// the same E4M3 values, and the tensor engine can fold s into its BF16 tiles
+// without a rounding (an E4M3 value times a power of two is a BF16 value).
 __global__ void scale_kernel(const unsigned *__restrict__ amax, float *__restrict__ scale, int64_t n)
 {
     const int64_t j = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (j < n) {
         const float a = __uint_as_float(amax[j]);
-        scale[j] = (a > 0.0f && a < INFINITY) ? a / 448.0f : 1.0f;
+        float s = 1.0f;
+        if (a > 0.0f && a < INFINITY) {
+            int e = 0;
+            const float mant = frexpf(a / 448.0f, &e); // a / 448 = mant * 2^e, mant in [0.5, 1)
+            s = ldexpf(1.0f, mant == 0.5f ? e - 1 : e);
+        }
+        scale[j] = s;
     }
 }
 
@@ -283,6 +305,19 @@ unsigned grid_for(int64_t items, int threads)
 }
 
 } // namespace
+
+cudaError_t launch_fp8_scales(const float *B, int64_t k, int64_t n, unsigned *amax, float *scale, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(amax, 0, sizeof(unsigned) * static_cast<size_t>(n), st);
+    if (e != cudaSuccess)
+        return e;
+    const int rows_per_cta = 256;
+    dim3 g(static_cast<unsigned>((n / 4 + 127) / 128), static_cast<unsigned>((k + rows_per_cta - 1) / rows_per_cta));
+    colmax_kernel<<<g, 128, 0, st>>>(B, k, n, amax, rows_per_cta);
+    scale_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(amax, scale, n);
+    count_launches(2);
+    return cudaGetLastError();
+}
 
 // Width constraint of each form on the FMA engine.
 int lowp_vec(gcoo_precision prec) { return prec == GCOO_PREC_BF16 ? 8 : prec == GCOO_PREC_SPLIT_BF16 ? 4 : 16; }
@@ -318,14 +353,10 @@ gcoo_status lowp_convert_b(gcoo_handle *h, const float *dB, int64_t n, gcoo_prec
                                                              reinterpret_cast<uint4 *>(w->split.ptr), n4);
         count_launches(1);
     } else {
-        GCOO_CUDA(cudaMemsetAsync(w->amax.ptr, 0, sizeof(unsigned) * n, st));
-        const int rows_per_cta = 256;
-        dim3 g(static_cast<unsigned>((n / 4 + 127) / 128), static_cast<unsigned>((h->k + rows_per_cta - 1) / rows_per_cta));
-        colmax_kernel<<<g, 128, 0, st>>>(dB, h->k, n, w->amax.ptr, rows_per_cta);
-        scale_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, st>>>(w->amax.ptr, w->scale.ptr, n);
+        GCOO_CUDA(launch_fp8_scales(dB, h->k, n, w->amax.ptr, w->scale.ptr, st));
         prep_fp8_kernel<<<grid_for(n4, 256), 256, 0, st>>>(reinterpret_cast<const float4 *>(dB), w->scale.ptr,
                                                            reinterpret_cast<uint32_t *>(w->f8.ptr), n4, n);
-        count_launches(3);
+        count_launches(1);
     }
     GCOO_LAUNCH("B conversion kernel");
     return GCOO_SUCCESS;

@@ -18,6 +18,8 @@
 // tensor memory, tcgen05.commit frees each slot, and all four warps drain the
 // accumulator with tcgen05.ld into C. Every wait is bounded.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_fp8.h>
 
 #include "handle.hpp"
 
@@ -39,6 +41,9 @@ struct TcPlan {
     // B workspace (per call)
     DevBuf<uint16_t> b_hi, b_lo;
     int64_t b_n = 0;
+    // FP8-B: per-column power-of-two scales (and their absmax scratch)
+    DevBuf<float> b_scale;
+    DevBuf<unsigned> b_amax;
 };
 
 void destroy_tc_plan(TcPlan *p) { delete p; }
@@ -151,8 +156,12 @@ __global__ void tile_fill_kernel(const Entry *__restrict__ packed, const int32_t
 }
 
 // B (k x n FP32, row-major) -> tiles [jt][cb] of N rows (output columns) x 16 k, swizzled.
+// With fp8_scale (FP8-B): each value is first quantized to E4M3 in units of
+// its column's power-of-two scale, then stored as the exact BF16 value of
+// E4M3 x scale, so the BF16 MMA multiplies the FP8-B operand exactly.
 __global__ void b_tiles_kernel(const float *__restrict__ B, int64_t k, int64_t n, int N, int64_t kb,
-                               __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo)
+                               __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo,
+                               const float *__restrict__ fp8_scale)
 {
     const int64_t cb = blockIdx.x;
     const int64_t jt = blockIdx.y;
@@ -163,7 +172,12 @@ __global__ void b_tiles_kernel(const float *__restrict__ B, int64_t k, int64_t n
         const int kk = idx / N;
         const int64_t c = cb * kTileK + kk;
         const int64_t j = jt * N + jj;
-        const float v = (c < k && j < n) ? __ldg(B + c * n + j) : 0.0f;
+        float v = (c < k && j < n) ? __ldg(B + c * n + j) : 0.0f;
+        if (fp8_scale && j < n) {
+            const float sc = fp8_scale[j];
+            const __nv_fp8_storage_t q = __nv_cvt_float_to_fp8(v / sc, __NV_SATFINITE, __NV_E4M3);
+            v = __half2float(__half(__nv_cvt_fp8_to_halfraw(q, __NV_E4M3))) * sc;
+        }
         const uint32_t off = sw32_offset(static_cast<uint32_t>(jj), static_cast<uint32_t>(kk)) / 2;
         const __nv_bfloat16 h = __float2bfloat16_rn(v);
         hi[tile * tile_elems + off] = h;
@@ -415,25 +429,29 @@ double tc_density(const gcoo_handle *h)
     return static_cast<double>(h->nnz) / (static_cast<double>(h->tc->tiles) * kPanel * kTileK);
 }
 
-gcoo_status tc_prepare_b(gcoo_handle *h, int64_t n)
+gcoo_status tc_prepare_b(gcoo_handle *h, int64_t n, bool fp8)
 {
     TcPlan &p = *h->tc;
     const int N = tile_n_for(n, p.split);
     const int64_t nt = (n + N - 1) / N;
     const size_t elems = static_cast<size_t>(nt) * p.kb * N * kTileK;
-    if (!p.b_hi.ensure(elems) || (p.split && !p.b_lo.ensure(elems)))
+    if (!p.b_hi.ensure(elems) || (p.split && !p.b_lo.ensure(elems)) ||
+        (fp8 && (!p.b_scale.ensure(static_cast<size_t>(n)) || !p.b_amax.ensure(static_cast<size_t>(n)))))
         return fail(GCOO_ERROR_ALLOC, "device allocation of the B tiles failed");
     p.b_n = n;
     return GCOO_SUCCESS;
 }
 
-gcoo_status tc_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, cudaStream_t st)
+gcoo_status tc_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, bool fp8, cudaStream_t st)
 {
     TcPlan &p = *h->tc;
     const int N = tile_n_for(n, p.split);
+    if (fp8)
+        GCOO_CUDA(launch_fp8_scales(dB, h->k, n, p.b_amax.ptr, p.b_scale.ptr, st));
     dim3 g(static_cast<unsigned>(p.kb), static_cast<unsigned>((n + N - 1) / N));
     b_tiles_kernel<<<g, 256, 0, st>>>(dB, h->k, n, N, p.kb, reinterpret_cast<__nv_bfloat16 *>(p.b_hi.ptr),
-                                      p.split ? reinterpret_cast<__nv_bfloat16 *>(p.b_lo.ptr) : nullptr);
+                                      p.split ? reinterpret_cast<__nv_bfloat16 *>(p.b_lo.ptr) : nullptr,
+                                      fp8 ? p.b_scale.ptr : nullptr);
     count_launches(1);
     GCOO_LAUNCH("b_tiles_kernel");
     cudaError_t e;

@@ -77,7 +77,31 @@ def test_auto_engine_choice(native, torch):
     assert blk.query_engine("bf16")
     rnd = native.GcooHandle(dev(torch, dg.bernoulli_dense(62, 512, 512, 0.01))).build()
     assert not rnd.query_engine("bf16")
-    assert not blk.query_engine("fp32") and not blk.query_engine("fp8_b")
+    assert not blk.query_engine("fp32") and blk.query_engine("fp8_b")
+    assert not rnd.query_engine("fp8_b")
+
+
+def test_tc_fp8_b(native, torch):
+    """FP8-B on the tensor engine: B quantized to E4M3 with power-of-two
+    column scales (the FMA engine's quantization), multiplied as exact BF16
+    values; columns of very different magnitude keep their accuracy, and the
+    two engines agree up to the BF16 rounding of A (the FMA engine keeps A in
+    FP32)."""
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.block_dense(64, 384, 320, 0.3)
+    B = dg.dense_pm1(64, 5, 320, 256)
+    B[:, :32] *= 1e-3
+    B[:, 32:64] *= 1e3
+    dA, dB = dev(torch, A), dev(torch, B)
+    ht = native.GcooHandle(dA).build()
+    assert ht.query_engine("fp8_b")
+    t = ht.spdm(dB, prec="fp8_b").cpu().numpy()
+    f = native.GcooHandle(dA, engine="cuda_core").build().spdm(dB, prec="fp8_b").cpu().numpy()
+    ref = exact(A, B)
+    for lo, hi in ((0, 32), (32, 64), (64, 256)):
+        err = rel_fro(t[:, lo:hi], ref[:, lo:hi])
+        assert 1e-4 < err <= 5e-2
+        assert rel_fro(t[:, lo:hi], f[:, lo:hi].astype(np.float64)) <= 1e-2
 
 
 def test_tc_matches_fma_engine_bf16(native, torch):
