@@ -48,18 +48,22 @@ def _check_f32(t, name, shape=None):
 
 
 class _DevArray:
-    """__cuda_array_interface__ wrapper: a torch view of library-owned memory."""
+    """__cuda_array_interface__ wrapper: a torch view of library-owned memory.
+    It holds its owner (the handle), and the tensor made from it holds the
+    wrapper, so the handle's arrays outlive every view of them; a later build
+    may still move them (views are of the arrays as built)."""
 
-    def __init__(self, ptr, n, typestr):
+    def __init__(self, ptr, n, typestr, owner=None):
+        self._owner = owner
         self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": typestr, "data": (int(ptr or 0), False),
                                          "version": 3, "strides": None}
 
 
-def _view_tensor(ptr, n, typestr):
+def _view_tensor(ptr, n, typestr, owner=None):
     torch = _torch()
     if n == 0 or not ptr:
         return torch.empty(0, dtype=torch.float32 if typestr == "<f4" else torch.int32, device="cuda")
-    return torch.as_tensor(_DevArray(ptr, n, typestr), device="cuda")
+    return torch.as_tensor(_DevArray(ptr, n, typestr, owner), device="cuda")
 
 
 FP32_ORDER = {"auto": 0, "rows": 1, "groups": 2}
@@ -133,11 +137,11 @@ class GcooHandle:
         check(lib().gcoo_export(self._h, C.byref(v)))
         ng = int(v.n_group)
         return {"m": v.m, "k": v.k, "nnz": int(v.nnz), "n_group": ng, "rows_per_group": v.rows_per_group,
-                "groupIndex": _view_tensor(v.group_index, ng + 1, "<i4"),
-                "nnzPerGroup": _view_tensor(v.nnz_per_group, ng + 1, "<i4"),
-                "vals": _view_tensor(v.vals, v.nnz, "<f4"),
-                "rows": _view_tensor(v.rows, v.nnz, "<i4"),
-                "cols": _view_tensor(v.cols, v.nnz, "<i4")}
+                "groupIndex": _view_tensor(v.group_index, ng + 1, "<i4", self),
+                "nnzPerGroup": _view_tensor(v.nnz_per_group, ng + 1, "<i4", self),
+                "vals": _view_tensor(v.vals, v.nnz, "<f4", self),
+                "rows": _view_tensor(v.rows, v.nnz, "<i4", self),
+                "cols": _view_tensor(v.cols, v.nnz, "<i4", self)}
 
     @property
     def nnz(self) -> int:

@@ -206,6 +206,34 @@ def test_staged_rebuild_overflowed_tiles(native, oracle_mod, torch):
     assert np.array_equal(h.spdm(dev(torch, B)).cpu().numpy().view(np.uint32), ref.view(np.uint32))
 
 
+def test_full_size_staged_rebuild_equals_two_pass(native, torch):
+    """n=8192, s=0.99: the staged rebuild (A read once, tiles staged and
+    placed) gives arrays bit-identical to the two-pass first build, also
+    after A changed so that some tiles overflow their slots (rescanned) --
+    compared with a fresh handle's two-pass build of the new A."""
+    from gcoospdm_gb300 import datagen as dg
+    dA = dg.bernoulli_dense_torch(8193, 8192, 8192, 0.01, device="cuda")
+    h = native.GcooHandle(dA).build()
+    first = {f: t.clone() for f, t in h.export().items() if f in FIELDS}
+    h.build()
+    again = h.export()
+    for f in FIELDS:
+        assert torch.equal(again[f], first[f]), f
+    assert h.check_arrays() == 0
+    # thin most rows out and fill a few tiles densely: same handle, staged path with rescans
+    dA[: 4096] *= (dg.bernoulli_dense_torch(8194, 4096, 8192, 0.5, device="cuda") != 0).float()
+    dA[100:104, 2048:3072] = dg.dense_pm1_torch(8195, 5, 4, 1024, device="cuda") + 2.0
+    dA[8190:8192, 7168:8192] = dg.dense_pm1_torch(8196, 5, 2, 1024, device="cuda") + 2.0
+    h.build()
+    got = h.export()
+    # a temporary handle: its exported views keep it (and its arrays) alive
+    ref = native.GcooHandle(dA).build().export()
+    assert got["nnz"] == ref["nnz"]
+    for f in FIELDS:
+        assert torch.equal(got[f], ref[f]), f
+    assert h.check_arrays() == 0
+
+
 def test_full_size_properties_8192(native, torch):
     """n=8192, s=0.99: counts equal the dense count, offsets are the exclusive
     prefix, every group is (column, row) sorted, values round-trip."""
