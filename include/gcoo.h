@@ -135,15 +135,19 @@ gcoo_status gcoo_create_coo(gcoo_handle **out, int64_t m, int64_t k, const int32
 
 /* build() (src/ShGCOOSpDM.cu:182-193): dense -> GCOO conversion into
  * handle-owned arrays (count, device exclusive scan, stable scatter). Reads
- * the total nnz back to size the arrays, so it synchronises `stream` once.
- * Calling it again re-converts (dA may have changed). */
+ * the total nnz back to size the arrays, so it synchronises `stream` once
+ * (twice for a matrix with skewed row lengths, whose long rows it lists).
+ * Calling it again re-converts (dA may have changed); a rebuild whose arrays
+ * have room reads dA once. */
 gcoo_status gcoo_build(gcoo_handle *h, void *stream);
 
 gcoo_status gcoo_export(const gcoo_handle *h, gcoo_view *out);
 
 /* runKernelTest() (src/ShGCOOSpDM.cu:195-213): C = A * B with the GCOO
  * built by gcoo_build, FP32 form. No allocation, no synchronisation; safe
- * to capture in a CUDA graph. dB is k x n, dC is m x n, row-major. */
+ * to capture in a CUDA graph. dB is k x n, dC is m x n, row-major. For a
+ * matrix with skewed row lengths the long rows run on a handle-owned stream
+ * forked from `stream` and joined back into it before the call returns. */
 gcoo_status gcoo_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, void *stream);
 
 /* The same multiply in another arithmetic form. The first call for a form
