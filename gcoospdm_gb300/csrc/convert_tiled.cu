@@ -253,19 +253,28 @@ seg_scatter_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t ti
 //   packed: row_ptr[r] + prefix[r][first segment] + rank of the entry in row r
 // and blocks past the staged ones rescan A for the overflowed tiles with the
 // two-pass scatter. Same arrays as the two-pass conversion, bit for bit.
-template <int CPG>
-__global__ void __launch_bounds__(kTileThreads, CPG <= 4 ? 8 : 6)
+// L columns per lane: 8 where the lane's CPG x 8 nonzero bits fit one word
+// (CPG <= 4), else 4. A warp then covers L / 4 segments and a tile's CTA has
+// 1024 / (32 L) warps: with L = 8 each warp's fixed costs (barriers, ranks,
+// the tile's bookkeeping) serve twice the columns and 4-warp CTAs fit 12 per
+// SM (192 KB of A in flight per SM against 128 KB with 8-warp CTAs).
+template <int CPG, int L>
+__global__ void __launch_bounds__(1024 / L, L == 8 ? 12 : (CPG <= 4 ? 8 : 6))
 stage_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t tiles, int64_t S, int32_t *__restrict__ cnt,
              unsigned long long *__restrict__ distinct, int32_t slot, uint2 *__restrict__ stage,
              int32_t *__restrict__ tile_tot, int32_t *__restrict__ over_list,
              unsigned long long *__restrict__ over_count, uint32_t *__restrict__ status)
 {
+    constexpr int kWarps = 1024 / L / 32;
+    constexpr int kSegPerWarp = L / 4;
+    static_assert(CPG * L <= 32, "a lane's nonzeros are one 32-bit mask");
+    static_assert(kWarps == 4 || kWarps == 8, "two int4 loads at most read the warp totals");
     // the tile's rows arrive by bulk copies: no registers held while they are in
     // flight, so a full complement of CTAs per SM keeps A streaming
     __shared__ __align__(128) float s_a[CPG][kTileCols];
     __shared__ __align__(8) uint64_t s_bar;
-    __shared__ __align__(16) int s_wtot[kSegsPerCta];
-    __shared__ int s_dist[kSegsPerCta];
+    __shared__ __align__(16) int s_wtot[8];
+    __shared__ int s_dist[8];
     __shared__ long long s_g; // the tile's group, computed once
     const int64_t b = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -283,16 +292,13 @@ stage_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t tiles, i
             bulk_g2s(s_a[r], A + (u0.r0 + r) * k + c0, bytes, &s_bar);
     }
     __syncthreads();
-    SegUnit u;
-    u.g = s_g;
-    {
-        const int64_t t = b - u.g * tiles;
-        u.s = t * kSegsPerCta + warp;
-        u.r0 = u.g * CPG;
-        u.nrows = static_cast<int>(u.r0 + CPG <= m ? CPG : m - u.r0);
-        u.c = u.s * kSegCols + static_cast<int64_t>(lane) * 4;
-        u.live = u.s * kSegCols < k;
-    }
+    const int64_t g = s_g;
+    const int64_t t = b - g * tiles;
+    const int64_t r0 = g * CPG;
+    const int nrows = static_cast<int>(r0 + CPG <= m ? CPG : m - r0);
+    const int sc = warp * (32 * L) + lane * L;                        // the lane's first column inside the tile
+    const int64_t c = t * kTileCols + sc;                              // ... in A
+    const int64_t s0 = t * (kTileCols / kSegCols) + warp * kSegPerWarp; // the warp's first segment
     // one warp polls the barrier, the others wait at the CTA barrier (no issue
     // slots spent); a wait that gives up (it never should) flags the build,
     // which the host then redoes on the two-pass path, once the copies landed
@@ -307,28 +313,40 @@ stage_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t tiles, i
         return;
     }
     // the lane's nonzeros as one mask in GCOO order: bit q * CPG + r = (row r, column c + q)
-    const int sc = warp * kSegCols + lane * 4; // the lane's first column inside the tile
     uint32_t msk = 0;
-    if (u.live && u.c < k) {
 #pragma unroll
-        for (int r = 0; r < CPG; ++r) {
-            if (r < u.nrows) {
-                const float4 x = *reinterpret_cast<const float4 *>(&s_a[r][sc]);
-                msk |= (nzb(x.x) << r) | (nzb(x.y) << (CPG + r)) | (nzb(x.z) << (2 * CPG + r)) |
-                       (nzb(x.w) << (3 * CPG + r));
+    for (int r = 0; r < CPG; ++r) {
+        if (r < nrows) {
+#pragma unroll
+            for (int h = 0; h < L / 4; ++h) {
+                if (c + 4 * h < k) { // k % 4 == 0: a float4 is wholly inside or wholly past the row
+                    const float4 x = *reinterpret_cast<const float4 *>(&s_a[r][sc + 4 * h]);
+                    const int q0 = 4 * h;
+                    msk |= (nzb(x.x) << (q0 * CPG + r)) | (nzb(x.y) << ((q0 + 1) * CPG + r)) |
+                           (nzb(x.z) << ((q0 + 2) * CPG + r)) | (nzb(x.w) << ((q0 + 3) * CPG + r));
+                }
             }
         }
     }
-    constexpr uint32_t kCol = (CPG == 8) ? 0x01010101u : (CPG == 4) ? 0x1111u : (CPG == 2) ? 0x55u : 0xfu;
-    int wsum = 0, my_cnt = 0;
+    constexpr uint32_t kCol = (CPG == 4) ? (L == 8 ? 0x11111111u : 0x1111u)
+                            : (CPG == 2) ? (L == 8 ? 0x5555u : 0x55u)
+                            : (CPG == 1) ? (L == 8 ? 0xffu : 0xfu) : 0x01010101u;
+    // per-row counts of the warp's segment(s): lanes 16..31 cover the second one (L = 8),
+    // so one reduction of (first | second << 16) counts both
+    const uint32_t hi = (L == 8 && lane >= 16) ? 16u : 0u;
+    int wsum = 0, my_a = 0, my_b = 0;
 #pragma unroll
     for (int r = 0; r < CPG; ++r) {
-        const int x = static_cast<int>(__reduce_add_sync(0xffffffffu, __popc(msk & (kCol << r))));
-        wsum += x;
-        my_cnt = lane == r ? x : my_cnt;
+        const uint32_t x = __reduce_add_sync(0xffffffffu, static_cast<uint32_t>(__popc(msk & (kCol << r))) << hi);
+        const int xa = static_cast<int>(x & 0xffffu), xb = static_cast<int>(x >> 16);
+        wsum += xa + xb;
+        my_a = lane == r ? xa : my_a;
+        my_b = lane == 16 + r ? xb : my_b;
     }
-    if (u.live && lane < u.nrows)
-        cnt[(u.r0 + lane) * S + u.s] = my_cnt; // lane r: row r's count
+    if (lane < nrows && s0 * kSegCols < k)
+        cnt[(r0 + lane) * S + s0] = my_a; // lane r: row r's count
+    if (L == 8 && lane >= 16 && lane - 16 < nrows && (s0 + 1) * kSegCols < k)
+        cnt[(r0 + lane - 16) * S + s0 + 1] = my_b;
     if (lane == 0) {
         s_wtot[warp] = wsum;
         s_dist[warp] = 0;
@@ -353,12 +371,15 @@ stage_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t tiles, i
     __syncthreads(); // every warp of the CTA reaches this (no early exit above)
     int off = 0, T = 0;
     {
-        static_assert(kSegsPerCta == 8, "two int4 loads read the warp totals");
+        int wt[8];
         const int4 w0 = *reinterpret_cast<const int4 *>(&s_wtot[0]);
-        const int4 w1 = *reinterpret_cast<const int4 *>(&s_wtot[4]);
-        const int wt[kSegsPerCta] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+        wt[0] = w0.x; wt[1] = w0.y; wt[2] = w0.z; wt[3] = w0.w;
+        if (kWarps == 8) {
+            const int4 w1 = *reinterpret_cast<const int4 *>(&s_wtot[4]);
+            wt[4] = w1.x; wt[5] = w1.y; wt[6] = w1.z; wt[7] = w1.w;
+        }
 #pragma unroll
-        for (int w = 0; w < kSegsPerCta; ++w) {
+        for (int w = 0; w < kWarps; ++w) {
             off += w < warp ? wt[w] : 0;
             T += wt[w];
         }
@@ -371,7 +392,7 @@ stage_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t tiles, i
         if (distinct) {
             int dsum = 0;
 #pragma unroll
-            for (int w = 0; w < kSegsPerCta; ++w)
+            for (int w = 0; w < kWarps; ++w)
                 dsum += s_dist[w];
             if (dsum)
                 atomicAdd(distinct, static_cast<unsigned long long>(dsum));
@@ -384,7 +405,7 @@ stage_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t tiles, i
         const int i = __ffs(msk) - 1;
         msk &= msk - 1u;
         const int q = i / CPG, r = i % CPG;
-        stage[pos++] = make_uint2((static_cast<uint32_t>(u.c + q) << 3) | static_cast<uint32_t>(r),
+        stage[pos++] = make_uint2((static_cast<uint32_t>(c + q) << 3) | static_cast<uint32_t>(r),
                                   __float_as_uint(s_a[r][sc + q]));
     }
 }
@@ -570,14 +591,14 @@ cudaError_t launch_stage(const float *A, int64_t m, int64_t k, int32_t cpg, int3
     if (units <= 0)
         return cudaSuccess;
     const unsigned grid = static_cast<unsigned>(units);
-#define GCOO_STAGE(C)                                                                                        \
-    stage_kernel<C><<<grid, kTileThreads, 0, st>>>(A, m, k, tiles, S, cnt, distinct, slot, stage, tile_tot, \
-                                                   over_list, over_count, status)
+#define GCOO_STAGE(C, L)                                                                                        \
+    stage_kernel<C, L><<<grid, 1024 / (L), 0, st>>>(A, m, k, tiles, S, cnt, distinct, slot, stage, tile_tot,   \
+                                                    over_list, over_count, status)
     switch (cpg) {
-    case 1: GCOO_STAGE(1); break;
-    case 2: GCOO_STAGE(2); break;
-    case 4: GCOO_STAGE(4); break;
-    case 8: GCOO_STAGE(8); break;
+    case 1: GCOO_STAGE(1, 8); break;
+    case 2: GCOO_STAGE(2, 8); break;
+    case 4: GCOO_STAGE(4, 8); break;
+    case 8: GCOO_STAGE(8, 4); break;
     default: return cudaErrorInvalidValue;
     }
 #undef GCOO_STAGE
