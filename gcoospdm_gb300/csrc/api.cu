@@ -283,7 +283,10 @@ gcoo_status finish_build(gcoo_handle *h, cudaStream_t st)
         GCOO_CUDA(cudaStreamSynchronize(st));
         h->n_long = std::min<int64_t>(h->readback[0], cap);
         if (h->n_long > 0 && !h->side) {
-            GCOO_CUDA(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+            // the long rows are the multiply's critical path: their CTAs go first
+            int lo = 0, hi = 0;
+            GCOO_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+            GCOO_CUDA(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, hi));
             GCOO_CUDA(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
             GCOO_CUDA(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
         }
