@@ -243,10 +243,10 @@ seg_scatter_kernel(const float *__restrict__ A, int64_t m, int64_t k, int64_t ti
 // ---- staged rebuild: A read once --------------------------------------------------
 // stage_kernel is seg_count_kernel that also keeps each tile's entries (a
 // tile: CPG rows x 1024 columns, one CTA, brought into shared memory by bulk
-// copies) in a fixed slot of `slot` entries,
-// in the tile's GCOO order (column, then row) and as (col << 3 | row in
-// group, value bits). tile_tot[b] = the tile's entry count, or -1 when it
-// overflowed its slot; an overflowed tile is appended to over_list instead.
+// copies) in a fixed slot of `slot` entries, in the tile's GCOO order
+// (column, then row), each as (col << 3 | row in group, value bits).
+// tile_tot[b] = the tile's entry count, or -1 when it overflowed its slot;
+// an overflowed tile is appended to over_list instead.
 // No CTA waits on another. place_kernel then runs after the segment prefix and
 // the row scan: one warp per staged tile copies its entries to
 //   GCOO:   group_index[g] + sum_r prefix[r][first segment of the tile] + i
