@@ -14,8 +14,9 @@
 //   * each lane then runs its column's chain over the batch from shared
 //     memory, in the row's column order starting from 0.0f -- the same fmaf
 //     chain as the row kernel and the reference, so results are bit-identical.
-// The row kernel (one row per CTA for skewed matrices) skips these rows: those
-// of at least long_row_min() = 256 entries.
+// Rows of at least long_row_min() = 256 entries come here; the others go to
+// spdm_short_kernel (spdm_fp32.cu), which runs beside this kernel on the
+// caller's stream while this one runs on the handle's side stream.
 #include "internal.cuh"
 
 namespace gcoo {
