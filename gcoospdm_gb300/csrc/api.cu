@@ -141,22 +141,25 @@ gcoo_status spdm_fp32(gcoo_handle *h, const float *dB, int64_t n, float *dC, cud
             p.depth = t.depth;
         }
     }
-    // a skewed matrix (tuned or overridden shapes aside): its long rows go to
-    // their own kernel, the short rest to a kernel without staging
+    // a skewed matrix (explicit launch-shape overrides aside): its long rows go
+    // to their own kernel, the short rest to a kernel without staging
     if (!override_params && h->n_long > 0 && h->side && long_rows_ok(n, dB)) {
         // the two kernels write disjoint rows of C: the long rows run on the
         // side stream, forked from and joined back into the caller's stream
         GCOO_CUDA(cudaEventRecord(h->ev_fork, st));
         GCOO_CUDA(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
-        cudaError_t e = launch_spdm_long(h->packed.ptr, h->row_ptr.ptr, h->long_rows.ptr, h->n_long, dB, n, dC,
-                                         h->side);
-        if (e != cudaSuccess)
-            return cuda_fail(e, "spdm_long_kernel launch");
-        e = launch_spdm_short(h->packed.ptr, h->row_ptr.ptr, h->m, dB, n, dC, long_row_min(), st);
-        if (e != cudaSuccess)
-            return cuda_fail(e, "spdm_short_kernel launch");
+        const cudaError_t el = launch_spdm_long(h->packed.ptr, h->row_ptr.ptr, h->long_rows.ptr, h->n_long, dB, n,
+                                                dC, h->side);
+        const cudaError_t es = el == cudaSuccess
+                                   ? launch_spdm_short(h->packed.ptr, h->row_ptr.ptr, h->m, dB, n, dC, long_row_min(), st)
+                                   : cudaSuccess;
+        // joined whatever happened: nothing of this call runs past it on the side stream
         GCOO_CUDA(cudaEventRecord(h->ev_join, h->side));
         GCOO_CUDA(cudaStreamWaitEvent(st, h->ev_join, 0));
+        if (el != cudaSuccess)
+            return cuda_fail(el, "spdm_long_kernel launch");
+        if (es != cudaSuccess)
+            return cuda_fail(es, "spdm_short_kernel launch");
         return GCOO_SUCCESS;
     }
     const LaunchShape s = pick_shape(p, h->m, n, h->nnz, h->max_row_nnz, reinterpret_cast<uintptr_t>(dB),
