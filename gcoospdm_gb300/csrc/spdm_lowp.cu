@@ -4,13 +4,15 @@
 // group and column tile, the group's entries staged to shared memory with
 // cp.async.bulk, one warp per row), with B read in a narrower format:
 //   BF16        B as bf16 (8 columns per 128-bit load), A values rounded to
-//               bf16, FP32 accumulation;
+//               bf16, FP32 accumulation (the mixed-precision bf16 FMA of
+//               sm_100+: no widening of the B values);
 //   SPLIT_BF16  B = Bh + Bl and a = ah + al as bf16 pairs; acc += ah*Bh +
 //               ah*Bl + al*Bh (three products, FP32 accumulation) -- FP32-level
 //               accuracy from bf16 operands;
-//   FP8_B       B as FP8 E4M3 scaled per column (s_j = max_c |B[c][j]| / 448),
-//               16 columns per 128-bit load, A kept FP32; the scale is applied
-//               once to the accumulated column.
+//   FP8_B       B as FP8 E4M3 scaled per column (s_j = the smallest power of
+//               two with max_c |B[c][j]| / s_j <= 448), 16 columns per 128-bit
+//               load, A kept FP32; the scale is applied once to the
+//               accumulated column.
 // B is converted into the handle's workspace by a pre-pass kernel per call.
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
