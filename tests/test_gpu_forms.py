@@ -1,7 +1,9 @@
-"""GPU: the reduced-precision forms on the FMA engine (BF16, split-BF16,
-FP8-B), each checked against the oracle: bit-identical for BF16 (the same
-fmaf chain on BF16-rounded inputs), within stated relative Frobenius bounds
-of FP64 for split-BF16 (1e-5) and FP8-B (5e-2)."""
+"""GPU: the reduced-precision forms (BF16, split-BF16, FP8-B), each checked
+against the oracle: bit-identical for BF16 and FP8-B on the FMA engine (the
+same fmaf chain on BF16-rounded, or E4M3-quantized and column-scaled,
+inputs), within stated relative Frobenius bounds of FP64 for split-BF16
+(1e-5) and FP8-B (5e-2), and FP8-B on the tensor engine within FP32 error of
+the product of its quantized operands."""
 from __future__ import annotations
 
 import numpy as np
@@ -27,6 +29,27 @@ def bf16_round(x):
     u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
     r = ((u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000).astype(np.uint32)
     return r.view(np.float32)
+
+
+def fp8_scales(B):
+    """Per-column power-of-two scales as the library computes them: the
+    smallest 2^e with absmax / 2^e <= 448, from the FP32 quotient absmax / 448."""
+    a = np.abs(np.asarray(B, np.float32)).max(axis=0)
+    r = (a / np.float32(448.0)).astype(np.float32)
+    mant, e = np.frexp(r)
+    e = np.where(mant == 0.5, e - 1, e)
+    s = np.ldexp(np.float32(1.0), e).astype(np.float32)
+    return np.where((a > 0) & np.isfinite(a), s, np.float32(1.0)).astype(np.float32)
+
+
+def e4m3_round(y):
+    """FP32 -> FP8 E4M3, round to nearest even, saturating at 448 (finite inputs)."""
+    y = np.asarray(y, np.float64)
+    a = np.abs(y)
+    e = np.floor(np.log2(np.where(a > 0, a, 1.0)))
+    step = np.ldexp(1.0, (np.maximum(e, -6) - 3).astype(np.int64))  # 3 mantissa bits; subnormal step 2^-9
+    q = np.minimum(np.round(a / step) * step, 448.0)
+    return (np.sign(y) * q).astype(np.float32)
 
 
 def rel_fro(Cm, C64):
@@ -95,6 +118,38 @@ def test_fp8_b_fma_engine(native, torch, problem):
     err = rel_fro(Cg, C64)
     assert err <= 5e-2
     assert err > 1e-4  # it really is the 3-bit-mantissa form
+
+
+def test_fp8_b_fma_engine_bit_identical_to_quantized_chain(native, oracle_mod, torch, problem):
+    """FP8-B on the FMA engine is the FP32 chain over B quantized to E4M3 in
+    units of a power-of-two column scale, times that scale: bit for bit the
+    oracle's chain over the quantized B, scaled afterwards (exact)."""
+    A, B, g, C64 = problem
+    B = B.copy()
+    B[:, :64] *= 1e-3  # columns of very different magnitude
+    B[:, 64:128] *= 1e3
+    s = fp8_scales(B)
+    Bq = e4m3_round(B / s)
+    ref = (oracle_mod.spdm(g, Bq) * s).astype(np.float32)
+    h = native.GcooHandle(dev(torch, A), engine="cuda_core").build()
+    Cg = h.spdm(dev(torch, B), prec="fp8_b").cpu().numpy()
+    assert np.array_equal(Cg.view(np.uint32), ref.view(np.uint32))
+
+
+def test_fp8_b_tensor_engine_matches_quantized_product(native, torch):
+    """FP8-B on the tensor engine: the same quantized B (exact in BF16), A in
+    BF16, FP32 accumulation in the tensor pipe -- within FP32 summation error
+    of the FP64 product of the quantized operands."""
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.block_dense(65, 384, 320, 0.3)
+    B = dg.dense_pm1(65, 5, 320, 256)
+    B[:, :32] *= 1e-3
+    s = fp8_scales(B)
+    ref = bf16_round(A).astype(np.float64) @ (e4m3_round(B / s).astype(np.float64) * s)
+    h = native.GcooHandle(dev(torch, A)).build()
+    assert h.query_engine("fp8_b")
+    Cg = h.spdm(dev(torch, B), prec="fp8_b").cpu().numpy()
+    assert rel_fro(Cg, ref) <= 1e-5
 
 
 def test_fp8_per_column_scales(native, torch, oracle_mod):
