@@ -24,7 +24,7 @@ namespace gcoo {
 namespace {
 
 constexpr int kBatch = 32;              // entries per batch: one per lane
-constexpr int kDepth = 6;               // B batches in flight
+constexpr int kDepth = 4;               // B batches in flight
 constexpr int kEntryDepth = 2 * kDepth; // entry batches on chip
 constexpr int kTileCols = 32;           // one column per lane
 static_assert(kEntryDepth >= 2 * kDepth - 1, "entries must land before their B pieces are requested");
