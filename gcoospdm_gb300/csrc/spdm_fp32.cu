@@ -290,7 +290,7 @@ spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ r
 // shuffled from the owning lanes; each column's fmaf chain runs over the row's
 // entries in column order from 0.0f, as in every other FP32 kernel.
 template <int V>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(64, 16)
 spdm_short_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ row_ptr, int64_t m,
                   const float *__restrict__ B, int64_t n, float *__restrict__ C, int32_t tiles, int32_t long_min)
 {
@@ -510,17 +510,19 @@ cudaError_t launch_spdm_short(const Entry *packed, const int32_t *row_ptr, int64
         v = 2;
     const int64_t tiles = (n + 32 * v - 1) / (32 * v);
     const int64_t warps = m * tiles;
-    const int64_t blocks = (warps + 7) / 8;
+    // two-warp CTAs: rows of very different lengths do not hold one another's
+    // CTA slot (8-warp CTAs: 145 us on the Zipf workload, 2-warp: 127 us, 1-warp: 134 us)
+    const int64_t blocks = (warps + 1) / 2;
     if (tiles > 0x7fffffffLL || blocks > 0x7fffffffLL)
         return cudaErrorInvalidConfiguration;
     const unsigned grid = static_cast<unsigned>(blocks);
     const int32_t nt = static_cast<int32_t>(tiles);
     if (v == 4)
-        spdm_short_kernel<4><<<grid, 256, 0, st>>>(packed, row_ptr, m, B, n, C, nt, long_min);
+        spdm_short_kernel<4><<<grid, 64, 0, st>>>(packed, row_ptr, m, B, n, C, nt, long_min);
     else if (v == 2)
-        spdm_short_kernel<2><<<grid, 256, 0, st>>>(packed, row_ptr, m, B, n, C, nt, long_min);
+        spdm_short_kernel<2><<<grid, 64, 0, st>>>(packed, row_ptr, m, B, n, C, nt, long_min);
     else
-        spdm_short_kernel<1><<<grid, 256, 0, st>>>(packed, row_ptr, m, B, n, C, nt, long_min);
+        spdm_short_kernel<1><<<grid, 64, 0, st>>>(packed, row_ptr, m, B, n, C, nt, long_min);
     count_launches(1);
     return cudaGetLastError();
 }
