@@ -306,6 +306,7 @@ spdm_short_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ 
     if (long_min > 0 && cnt >= long_min)
         return; // the long-row kernel writes this row (warp-uniform)
     const bool has_col = j < n;
+    const bool all_cols = __all_sync(0xffffffffu, has_col);
     const float *Bj = B + (has_col ? j : 0);
     float acc[V];
 #pragma unroll
@@ -318,7 +319,26 @@ spdm_short_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ 
         my.val = 0.0f;
         if (lane < nw)
             my = packed[rs + w0 + lane];
-        for (int u0 = 0; u0 < nw; u0 += 8) {
+        int u0 = 0;
+        if (all_cols) { // warp-uniform: every lane takes part in the shuffles below
+            // whole batches of eight: no per-entry predicates
+            for (; u0 + 8 <= nw; u0 += 8) {
+                float a[8], b[8][V];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int col = __shfl_sync(0xffffffffu, my.col, u0 + u);
+                    a[u] = __shfl_sync(0xffffffffu, my.val, u0 + u);
+                    Vec<V>::load(Bj + static_cast<int64_t>(col) * n, b[u]);
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+#pragma unroll
+                    for (int v = 0; v < V; ++v)
+                        acc[v] = fmaf(a[u], b[u][v], acc[v]);
+            }
+        }
+        // the tail batch (and lanes past n: shuffles only)
+        for (; u0 < nw; u0 += 8) {
             float a[8], b[8][V];
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
