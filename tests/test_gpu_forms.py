@@ -9,6 +9,8 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
+from fp8_emu import e4m3_round, fp8_scales
+
 pytestmark = pytest.mark.gpu
 
 
@@ -29,27 +31,6 @@ def bf16_round(x):
     u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
     r = ((u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000).astype(np.uint32)
     return r.view(np.float32)
-
-
-def fp8_scales(B):
-    """Per-column power-of-two scales as the library computes them: the
-    smallest 2^e with absmax / 2^e <= 448, from the FP32 quotient absmax / 448."""
-    a = np.abs(np.asarray(B, np.float32)).max(axis=0)
-    r = (a / np.float32(448.0)).astype(np.float32)
-    mant, e = np.frexp(r)
-    e = np.where(mant == 0.5, e - 1, e)
-    s = np.ldexp(np.float32(1.0), e).astype(np.float32)
-    return np.where((a > 0) & np.isfinite(a), s, np.float32(1.0)).astype(np.float32)
-
-
-def e4m3_round(y):
-    """FP32 -> FP8 E4M3, round to nearest even, saturating at 448 (finite inputs)."""
-    y = np.asarray(y, np.float64)
-    a = np.abs(y)
-    e = np.floor(np.log2(np.where(a > 0, a, 1.0)))
-    step = np.ldexp(1.0, (np.maximum(e, -6) - 3).astype(np.int64))  # 3 mantissa bits; subnormal step 2^-9
-    q = np.minimum(np.round(a / step) * step, 448.0)
-    return (np.sign(y) * q).astype(np.float32)
 
 
 def rel_fro(Cm, C64):
