@@ -277,6 +277,35 @@ def test_multiply_by_steady_state_and_determinism(native, torch):
     assert torch.equal(C1, C2) and torch.equal(C1, C3)
 
 
+def test_multiply_by_on_changing_matrices(native, oracle_mod, torch):
+    """mutiplyBy with A's contents changing between calls: rebuilds with
+    room (staged), denser than the arrays' room (the staged attempt falls
+    back to the two-pass build), skewed (the long/short split), back to
+    sparse. Every result is bit-identical to the oracle's."""
+    from gcoospdm_gb300 import datagen as dg
+    m, k, n = 1500, 2048, 256
+    rng = np.random.default_rng(77)
+    sparse = dg.bernoulli_dense(71, m, k, 0.01)
+    dense = dg.bernoulli_dense(72, m, k, 0.2)
+    skewed = dg.bernoulli_dense(73, m, k, 0.005)
+    for r, length in ((5, 1500), (600, 800), (1499, 300)):
+        cols = np.sort(rng.choice(k, size=length, replace=False))
+        v = rng.uniform(-1.0, 1.0, size=length).astype(np.float32)
+        skewed[r, :] = 0.0
+        skewed[r, cols] = np.where(v == 0.0, np.float32(0.5), v)
+    B = dg.dense_pm1(74, 1, k, n)
+    dA, dB = dev(torch, sparse), dev(torch, B)
+    h = native.GcooHandle(dA)
+    Cd = torch.empty(m, n, device="cuda")
+    for A in (sparse, sparse, dense, dense, skewed, skewed, sparse):
+        dA.copy_(dev(torch, A))
+        Cd.fill_(float("nan"))
+        h.multiply_by(dB, Cd)
+        ref = oracle_mod.spdm(oracle_mod.convert(A), B)
+        assert same_bits(Cd.cpu().numpy(), ref)
+        assert h.device_status() == 0
+
+
 def test_error_norm_kernel_matches_oracle(native, oracle_mod, torch):
     from gcoospdm_gb300 import datagen as dg
     A = dg.bernoulli_dense(27, 500, 400, 0.05)
