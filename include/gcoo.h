@@ -44,7 +44,7 @@ typedef enum gcoo_status {
     GCOO_ERROR_ALLOC = 2,         /* device allocation failed             */
     GCOO_ERROR_CUDA = 3,          /* a CUDA call or kernel launch failed  */
     GCOO_ERROR_NOT_BUILT = 4,     /* multiply before gcoo_build           */
-    GCOO_ERROR_UNSUPPORTED = 5,   /* request this build cannot serve      */
+    GCOO_ERROR_UNSUPPORTED = 5,   /* request this library cannot serve    */
     GCOO_ERROR_FORMAT = 6,        /* nnz does not fit the int32 format    */
     GCOO_ERROR_TIMEOUT = 7,       /* a bounded device wait gave up        */
     GCOO_ERROR_CAPACITY = 8       /* caller-provided buffer too small     */
