@@ -138,7 +138,9 @@ gcoo_status gcoo_create_coo(gcoo_handle **out, int64_t m, int64_t k, const int32
  * the total nnz back to size the arrays, so it synchronises `stream` once
  * (twice for a matrix with skewed row lengths, whose long rows it lists).
  * Calling it again re-converts (dA may have changed); a rebuild whose arrays
- * have room reads dA once. */
+ * have room reads dA once. A matrix of more than 2^31 - 1 nonzeros does not
+ * fit the format's int32 offsets: refused with GCOO_ERROR_FORMAT before any
+ * entry is written, leaving the handle unbuilt. */
 gcoo_status gcoo_build(gcoo_handle *h, void *stream);
 
 gcoo_status gcoo_export(const gcoo_handle *h, gcoo_view *out);
@@ -147,7 +149,11 @@ gcoo_status gcoo_export(const gcoo_handle *h, gcoo_view *out);
  * built by gcoo_build, FP32 form. No allocation, no synchronisation; safe
  * to capture in a CUDA graph. dB is k x n, dC is m x n, row-major. For a
  * matrix with skewed row lengths the long rows run on a handle-owned stream
- * forked from `stream` and joined back into it before the call returns. */
+ * forked from `stream` and joined back into it before the call returns.
+ * Column tiles lie along the grid's y dimension, as in the reference's
+ * launch (src/ShGCOOSpDM.cu:153): n up to 65535 tiles of the chosen shape
+ * (16.7 M columns at the default shape when n % 4 == 0); wider B fails with
+ * GCOO_ERROR_CUDA. */
 gcoo_status gcoo_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, void *stream);
 
 /* The same multiply in another arithmetic form. The first call for a form

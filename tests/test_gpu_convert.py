@@ -253,3 +253,45 @@ def test_full_size_properties_8192(native, torch):
     key = grp * (1 << 40) + cols * 8192 + rows
     assert bool((key[1:] > key[:-1]).all())
     assert torch.equal(dA[rows, cols], a["vals"])
+
+
+@pytest.mark.parametrize("n", [46344, 46341])
+def test_nnz_beyond_int32_refused_and_handle_recovers(native, torch, n):
+    """A dense n x n matrix of ones holds n*n > 2^31 - 1 nonzeros (8.6 GB),
+    more than the format's int32 offsets can address. Every conversion entry
+    refuses it with GCOO_ERROR_FORMAT (6) before writing an entry: the first
+    two-pass build, the caller-array count, and a later one-read rebuild of
+    a handle whose arrays exist (n = 46344; k odd takes the scalar count).
+    The handle stays usable: a refused rebuild leaves it unbuilt, and once A
+    is thinned out it builds and multiplies."""
+    A = torch.ones(n, n, device="cuda")
+    h = native.GcooHandle(A)
+    with pytest.raises(native.GcooError) as e:
+        h.build()
+    assert e.value.status == 6
+    ng = (n + 3) // 4
+    with pytest.raises(native.GcooError) as e:
+        native.convert_count(A)
+    assert e.value.status == 6
+    A[1:] = 0.0
+    h.build()
+    assert h.nnz == n and h.check_arrays() == 0 and h.device_status() == 0
+    A.fill_(1.0)
+    with pytest.raises(native.GcooError) as e:
+        h.build()
+    assert e.value.status == 6
+    B = torch.ones(n, 8, device="cuda")
+    with pytest.raises(native.GcooError) as e:
+        h.spdm(B)
+    assert e.value.status == 4  # not built: the refused build left no stale arrays in use
+    A.zero_()
+    A[:, 0] = 2.0
+    h.build()
+    a = h.export()
+    assert a["nnz"] == n and a["n_group"] == ng
+    assert torch.equal(a["cols"], torch.zeros(n, dtype=torch.int32, device="cuda"))
+    assert torch.equal(h.spdm(B), torch.full((n, 8), 2.0, device="cuda"))
+    assert h.device_status() == 0 and h.check_arrays() == 0
+    h.close()
+    del h, A
+    torch.cuda.empty_cache()
