@@ -143,7 +143,7 @@ gcoo_status spdm_fp32(gcoo_handle *h, const float *dB, int64_t n, float *dC, cud
     }
     // a skewed matrix (explicit launch-shape overrides aside): its long rows go
     // to their own kernel, the short rest to a kernel without staging
-    if (!override_params && h->n_long > 0 && h->side && long_rows_ok(n, dB)) {
+    if (!override_params && h->n_long > 0 && h->side && h->ev_fork && h->ev_join && long_rows_ok(n, dB)) {
         // the two kernels write disjoint rows of C: the long rows run on the
         // side stream, forked from and joined back into the caller's stream
         GCOO_CUDA(cudaEventRecord(h->ev_fork, st));
@@ -285,13 +285,23 @@ gcoo_status finish_build(gcoo_handle *h, cudaStream_t st)
         GCOO_CUDA(cudaMemcpyAsync(h->readback, d_cnt, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
         GCOO_CUDA(cudaStreamSynchronize(st));
         h->n_long = std::min<int64_t>(h->readback[0], cap);
-        if (h->n_long > 0 && !h->side) {
+        if (h->n_long > 0) {
             // the long rows are the multiply's critical path: their CTAs go first
-            int lo = 0, hi = 0;
-            GCOO_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-            GCOO_CUDA(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, hi));
-            GCOO_CUDA(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
-            GCOO_CUDA(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+            // (each object made once; one that failed is retried by the next build)
+            if (!h->side) {
+                int lo = 0, hi = 0;
+                cudaStream_t side = nullptr;
+                GCOO_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+                GCOO_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi));
+                h->side = side;
+            }
+            for (cudaEvent_t *ev : {&h->ev_fork, &h->ev_join}) {
+                if (*ev)
+                    continue;
+                cudaEvent_t made = nullptr;
+                GCOO_CUDA(cudaEventCreateWithFlags(&made, cudaEventDisableTiming));
+                *ev = made;
+            }
         }
     }
     h->built = true;

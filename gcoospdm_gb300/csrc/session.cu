@@ -127,77 +127,13 @@ gcoo_status ensure_events(gcoo_session *s, size_t panels)
     return GCOO_SUCCESS;
 }
 
-} // namespace
-
-} // namespace gcoo
-
-using namespace gcoo;
-
-extern "C" {
-
-gcoo_status gcoo_session_create(gcoo_session **out, const gcoo_params *params, int64_t panel_rows)
+// The copies and launches of one session multiply, in stream order (no waits
+// on the host); an error returns at once and the caller drains the streams.
+gcoo_status session_enqueue(gcoo_session *s, const float *hA, int64_t k, const float *hB, int64_t n, float *hC,
+                            cudaStream_t user, const std::vector<int64_t> &starts, int64_t P, int lanes)
 {
-    if (!out)
-        return fail(GCOO_ERROR_INVALID_VALUE, "out is NULL");
-    *out = nullptr;
-    if (panel_rows < 0)
-        return fail(GCOO_ERROR_INVALID_VALUE, "panel_rows must be >= 0");
-    gcoo_params p;
-    gcoo_params_default(&p);
-    if (params)
-        p = *params;
-    const int32_t c = p.rows_per_group;
-    if (!(c == 1 || c == 2 || c == 4 || c == 8 || c == 16 || c == 32))
-        return fail(GCOO_ERROR_INVALID_VALUE, "rows_per_group must be 1, 2, 4, 8, 16 or 32");
-    gcoo_session *s = new gcoo_session();
-    s->p = p;
-    s->panel_rows_req = panel_rows;
-    if (cudaStreamCreateWithFlags(&s->s_in, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&s->lane[0].s, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&s->lane[1].s, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&s->s_out, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&s->ev_start, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&s->ev_b, cudaEventDisableTiming) != cudaSuccess) {
-        delete s;
-        return fail(GCOO_ERROR_CUDA, "stream or event creation failed");
-    }
-    *out = s;
-    return GCOO_SUCCESS;
-}
-
-gcoo_status gcoo_session_multiply(gcoo_session *s, const float *hA, int64_t m, int64_t k, const float *hB,
-                                  int64_t n, float *hC, void *stream)
-{
-    NvtxRange nvtx("gcoo_session_multiply");
-    if (!s || !hA || !hB || !hC)
-        return fail(GCOO_ERROR_INVALID_VALUE, "NULL session or matrix pointer");
-    if (m <= 0 || k <= 0 || m >= (int64_t(1) << 31) || k >= (int64_t(1) << 31))
-        return fail(GCOO_ERROR_INVALID_VALUE, "m and k must be in [1, 2^31)");
-    if (n <= 0 || n >= (int64_t(1) << 31))
-        return fail(GCOO_ERROR_INVALID_VALUE, "n must be in [1, 2^31)");
     const int32_t cpg = s->p.rows_per_group;
-    const int64_t P = pick_panel_rows(m, k, cpg, s->panel_rows_req);
-    const std::vector<int64_t> starts = panel_starts(m, cpg, P, s->panel_rows_req == 0);
     const int64_t panels = static_cast<int64_t>(starts.size()) - 1;
-    const int64_t cap = P * k; // dense panel: the most entries a panel can have
-
-    if (!s->dA.ensure(static_cast<size_t>(m * k)) || !s->dB.ensure(static_cast<size_t>(k * n)) ||
-        !s->dC.ensure(static_cast<size_t>(m * n)) || !s->status.ensure(1))
-        return fail(GCOO_ERROR_ALLOC, "device allocation of the session buffers failed");
-    const int lanes = panels > 1 ? kLanes : 1;
-    for (int l = 0; l < lanes; ++l) {
-        SessionLane &L = s->lane[l];
-        if (!L.row_ptr.ensure(static_cast<size_t>(P) + 1) || !L.packed.ensure(static_cast<size_t>(cap) + 2) ||
-            !L.scratch.ensure(scan_scratch_elems(P) + 2) ||
-            !L.tile_cnt.ensure(static_cast<size_t>(P * conv_segments(k))))
-            return fail(GCOO_ERROR_ALLOC, "device allocation of the session workspace failed");
-    }
-    gcoo_status st = ensure_events(s, static_cast<size_t>(panels));
-    if (st != GCOO_SUCCESS)
-        return st;
-
-    const uint64_t launches0 = gcoo_kernel_launches();
-    cudaStream_t user = static_cast<cudaStream_t>(stream);
     GCOO_CUDA(cudaEventRecord(s->ev_start, user));
     GCOO_CUDA(cudaStreamWaitEvent(s->s_in, s->ev_start, 0));
     GCOO_CUDA(cudaMemsetAsync(s->status.ptr, 0, sizeof(uint32_t), s->s_in));
@@ -255,10 +191,103 @@ gcoo_status gcoo_session_multiply(gcoo_session *s, const float *hA, int64_t m, i
         GCOO_CUDA(cudaMemcpyAsync(hC + r0 * n, dC + r0 * n, static_cast<size_t>(rows * n) * sizeof(float),
                                   cudaMemcpyDeviceToHost, s->s_out));
     }
-    for (int l = 0; l < lanes; ++l)
-        GCOO_CUDA(cudaStreamSynchronize(s->lane[l].s));
-    GCOO_CUDA(cudaStreamSynchronize(s->s_out));
-    GCOO_CUDA(cudaStreamSynchronize(s->s_in));
+    return GCOO_SUCCESS;
+}
+
+} // namespace
+
+} // namespace gcoo
+
+using namespace gcoo;
+
+extern "C" {
+
+gcoo_status gcoo_session_create(gcoo_session **out, const gcoo_params *params, int64_t panel_rows)
+{
+    if (!out)
+        return fail(GCOO_ERROR_INVALID_VALUE, "out is NULL");
+    *out = nullptr;
+    if (panel_rows < 0)
+        return fail(GCOO_ERROR_INVALID_VALUE, "panel_rows must be >= 0");
+    gcoo_params p;
+    gcoo_params_default(&p);
+    if (params)
+        p = *params;
+    const int32_t c = p.rows_per_group;
+    if (!(c == 1 || c == 2 || c == 4 || c == 8 || c == 16 || c == 32))
+        return fail(GCOO_ERROR_INVALID_VALUE, "rows_per_group must be 1, 2, 4, 8, 16 or 32");
+    gcoo_session *s = new gcoo_session();
+    s->p = p;
+    s->panel_rows_req = panel_rows;
+    if (cudaStreamCreateWithFlags(&s->s_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->lane[0].s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->lane[1].s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s->s_out, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_start, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_b, cudaEventDisableTiming) != cudaSuccess) {
+        delete s;
+        return fail(GCOO_ERROR_CUDA, "stream or event creation failed");
+    }
+    *out = s;
+    return GCOO_SUCCESS;
+}
+
+gcoo_status gcoo_session_multiply(gcoo_session *s, const float *hA, int64_t m, int64_t k, const float *hB,
+                                  int64_t n, float *hC, void *stream)
+{
+    NvtxRange nvtx("gcoo_session_multiply");
+    if (!s || !hA || !hB || !hC)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL session or matrix pointer");
+    if (m <= 0 || k <= 0 || m >= (int64_t(1) << 31) || k >= (int64_t(1) << 31))
+        return fail(GCOO_ERROR_INVALID_VALUE, "m and k must be in [1, 2^31)");
+    if (n <= 0 || n >= (int64_t(1) << 31))
+        return fail(GCOO_ERROR_INVALID_VALUE, "n must be in [1, 2^31)");
+    const int32_t cpg = s->p.rows_per_group;
+    const int64_t P = pick_panel_rows(m, k, cpg, s->panel_rows_req);
+    const std::vector<int64_t> starts = panel_starts(m, cpg, P, s->panel_rows_req == 0);
+    const int64_t panels = static_cast<int64_t>(starts.size()) - 1;
+    int64_t tallest = 0;
+    for (int64_t q = 0; q < panels; ++q)
+        tallest = std::max(tallest, starts[q + 1] - starts[q]);
+    const int64_t cap = tallest * k; // dense panel: the most entries a panel can have
+    // A panel is scattered without a readback of its total, so even a dense
+    // panel must fit the int32 offsets. Only k of about 2^31 / rows_per_group
+    // columns or more, where a panel is one group high, can break this;
+    // gcoo_build checks the total before it scatters and takes such matrices.
+    if (cap > 0x7fffffffLL - 2)
+        return fail(GCOO_ERROR_UNSUPPORTED, "k too large for a host-buffer panel within the int32 format: "
+                                            "use gcoo_create + gcoo_build");
+
+    if (!s->dA.ensure(static_cast<size_t>(m * k)) || !s->dB.ensure(static_cast<size_t>(k * n)) ||
+        !s->dC.ensure(static_cast<size_t>(m * n)) || !s->status.ensure(1))
+        return fail(GCOO_ERROR_ALLOC, "device allocation of the session buffers failed");
+    const int lanes = panels > 1 ? kLanes : 1;
+    for (int l = 0; l < lanes; ++l) {
+        SessionLane &L = s->lane[l];
+        if (!L.row_ptr.ensure(static_cast<size_t>(P) + 1) || !L.packed.ensure(static_cast<size_t>(cap) + 2) ||
+            !L.scratch.ensure(scan_scratch_elems(P) + 2) ||
+            !L.tile_cnt.ensure(static_cast<size_t>(P * conv_segments(k))))
+            return fail(GCOO_ERROR_ALLOC, "device allocation of the session workspace failed");
+    }
+    gcoo_status st = ensure_events(s, static_cast<size_t>(panels));
+    if (st != GCOO_SUCCESS)
+        return st;
+
+    const uint64_t launches0 = gcoo_kernel_launches();
+    cudaStream_t user = static_cast<cudaStream_t>(stream);
+    const gcoo_status enq = session_enqueue(s, hA, k, hB, n, hC, user, starts, P, lanes);
+    // whatever was enqueued has finished before the call returns, also after
+    // an error: nothing of it may still read hA / hB or write hC afterwards
+    cudaError_t drained = cudaSuccess;
+    for (cudaStream_t q : {s->lane[0].s, s->lane[1].s, s->s_out, s->s_in}) {
+        const cudaError_t e = cudaStreamSynchronize(q);
+        if (drained == cudaSuccess)
+            drained = e;
+    }
+    if (enq != GCOO_SUCCESS)
+        return enq;
+    if (drained != cudaSuccess)
+        return cuda_fail(drained, "session stream synchronisation");
     uint32_t status = 0;
     GCOO_CUDA(cudaMemcpy(&status, s->status.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     s->last_launches = static_cast<int32_t>(gcoo_kernel_launches() - launches0);
@@ -269,6 +298,7 @@ gcoo_status gcoo_session_multiply(gcoo_session *s, const float *hA, int64_t m, i
         return fail(GCOO_ERROR_TIMEOUT, "a bounded device wait gave up");
     return GCOO_SUCCESS;
 }
+
 
 gcoo_status gcoo_session_stats(const gcoo_session *s, int32_t *launches, int32_t *panels)
 {

@@ -152,8 +152,9 @@ gcoo_status gcoo_export(const gcoo_handle *h, gcoo_view *out);
  * forked from `stream` and joined back into it before the call returns.
  * Column tiles lie along the grid's y dimension, as in the reference's
  * launch (src/ShGCOOSpDM.cu:153): n up to 65535 tiles of the chosen shape
- * (16.7 M columns at the default shape when n % 4 == 0); wider B fails with
- * GCOO_ERROR_CUDA. */
+ * (16.7 M columns at the default shape when n % 4 == 0, more where short
+ * rows walk several tiles per CTA); wider B fails with GCOO_ERROR_CUDA
+ * before any launch. */
 gcoo_status gcoo_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, void *stream);
 
 /* The same multiply in another arithmetic form. The first call for a form
@@ -292,14 +293,20 @@ gcoo_status gcoo_batch_destroy(gcoo_batch *b);
 typedef struct gcoo_session gcoo_session;
 
 /* panel_rows: rows of A per panel (rounded up to rows_per_group); 0 picks
- * about 16 panels. Allocates nothing until the first multiply. */
+ * eighth-of-A panels, with a quarter-size panel first and halving ones at
+ * the end (about a dozen in all). Allocates nothing until the first
+ * multiply. */
 gcoo_status gcoo_session_create(gcoo_session **out, const gcoo_params *params, int64_t panel_rows);
 
 /* C = A x B, A m x k, B k x n, C m x n, all row-major FP32 in HOST memory
  * (page-locked memory moves at full link speed; pageable memory works, more
  * slowly). Device buffers grow to the largest call and are reused, so a
  * steady loop allocates nothing. Work is ordered after what was queued on
- * `stream` before the call; returns once C is complete on the host. */
+ * `stream` before the call; returns once C is complete on the host, and on
+ * an error only once nothing of the call is still running. A panel is
+ * scattered without a readback, so k of about 2^31 / rows_per_group
+ * columns or more, where one panel could exceed the int32 format, is
+ * refused with GCOO_ERROR_UNSUPPORTED (gcoo_build takes such matrices). */
 gcoo_status gcoo_session_multiply(gcoo_session *s, const float *hA, int64_t m, int64_t k, const float *hB,
                                   int64_t n, float *hC, void *stream);
 

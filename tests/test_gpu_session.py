@@ -112,3 +112,36 @@ def test_session_full_size_matches_multiply_by(native, torch):
     assert torch.equal(Ch.view(torch.int32), Cd.cpu().view(torch.int32))
     assert s.stats()["panels"] == 11  # 6 full 1024-row panels, then 1024, 512, 256, 128, 128
     s.close()
+
+
+def test_session_refuses_panels_beyond_int32(native, torch):
+    """k = 2^26 + 1 columns in 32-row groups: a one-group panel could hold
+    more than 2^31 - 1 entries, which a panel (scattered without a readback
+    of its total) cannot take. Refused with GCOO_ERROR_UNSUPPORTED before any
+    allocation or copy; the host buffers are allocated but never touched."""
+    k = (1 << 26) + 1
+    A = torch.empty((32, k), dtype=torch.float32)
+    B = torch.empty((k, 1), dtype=torch.float32)
+    s = native.GcooSession(rows_per_group=32)
+    with pytest.raises(native.GcooError) as e:
+        s.multiply(A, B)
+    assert e.value.status == 5
+    s.close()
+
+
+def test_session_error_after_enqueue_drains_and_recovers(native, torch):
+    """B wider than 65535 column tiles (n odd: 64-column tiles): the first
+    panel's multiply is refused on the host after the copies of A and B were
+    enqueued. The call drains its streams before it returns
+    GCOO_ERROR_CUDA, and the session then multiplies normally."""
+    from gcoospdm_gb300 import datagen as dg
+    A = torch.from_numpy(dg.bernoulli_dense(41, 8, 4, 0.6))
+    n = 65535 * 64 + 1
+    s = native.GcooSession()
+    with pytest.raises(native.GcooError) as e:
+        s.multiply(A, torch.ones((4, n), dtype=torch.float32))
+    assert e.value.status == 3
+    B = torch.from_numpy(dg.dense_pm1(41, 5, 4, 33))
+    C = s.multiply(A, B)
+    assert same_bits(torch, C, device_result(native, torch, A, B))
+    s.close()
