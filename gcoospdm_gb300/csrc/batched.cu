@@ -356,9 +356,12 @@ gcoo_status gcoo_batch_create(gcoo_batch **out, const gcoo_problem *problems, in
     for (int32_t i = 0; i < count; ++i)
         by_bucket[b->bucket[i]].push_back(i);
     std::map<std::string, int> rpi;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0)
+            cudaEventDestroy(e0);
+        return bail(fail(GCOO_ERROR_CUDA, "event creation for batch tuning failed"));
+    }
     for (auto &kv : by_bucket) {
         const std::string key = kv.first + (prec == GCOO_PREC_BF16 ? "_bf16" : "_fp32");
         TuneEntry te;
@@ -372,8 +375,12 @@ gcoo_status gcoo_batch_create(gcoo_batch **out, const gcoo_problem *problems, in
             std::map<std::string, int> one = {{kv.first, r}};
             std::vector<BatchItem> items;
             make_items(*b, kv.second, one, items);
-            if (upload_items(*b, items, st) != GCOO_SUCCESS)
-                return bail(GCOO_ERROR_ALLOC);
+            const gcoo_status us = upload_items(*b, items, st);
+            if (us != GCOO_SUCCESS) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return bail(us);
+            }
             float ms_min = 1e30f;
             for (int rep = 0; rep < 3; ++rep) {
                 cudaMemsetAsync(b->counter.ptr, 0, sizeof(unsigned), st);

@@ -268,7 +268,9 @@ typedef struct gcoo_batch gcoo_batch;
 /* Plans many independent multiplies for one persistent launch: work items
  * (problem, group range, column tile) sorted by nnz, descending, in a device
  * queue; tile parameters per shape bucket from the autotune table when one is
- * loaded. prec: GCOO_PREC_FP32 or GCOO_PREC_BF16. Allocates; synchronises. */
+ * loaded, else timed here by running the batch's items (which writes the
+ * problems' C) and stored in the table. prec: GCOO_PREC_FP32 or
+ * GCOO_PREC_BF16. Allocates; synchronises. */
 gcoo_status gcoo_batch_create(gcoo_batch **out, const gcoo_problem *problems, int32_t count,
                               gcoo_precision prec, void *stream);
 
