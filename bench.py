@@ -144,27 +144,35 @@ def measured_peaks():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling around the timed region (every 20 ms, timestamped);
+    the summary keeps the samples taken inside the region that mark() names."""
+
+    SAMPLE_MS = 20
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
         self.path = None
+        self.window = None
 
     def __enter__(self):
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
-        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.SAMPLE_MS)],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
         time.sleep(0.3)
         return self
+
+    def mark(self, t0: float, t1: float):
+        """The timed region in host wall-clock seconds (time.time())."""
+        self.window = (t0, t1)
 
     def __exit__(self, *a):
         if self.proc is not None:
@@ -177,24 +185,33 @@ class Clocks:
     def summary(self):
         if self.proc is None or not self.path:
             return None
-        rows = []
+        import datetime
+        rows = []  # (time, sm MHz, max MHz, reason flags, power W)
         with open(self.path) as f:
             for line in f:
                 p = [x.strip() for x in line.split(",")]
-                if len(p) < 9:
+                if len(p) < 10:
                     continue
                 try:
-                    rows.append((float(p[1]), float(p[2]), p[5:9], float(p[3]) if p[3] not in ("[N/A]", "") else 0.0))
+                    ts = datetime.datetime.strptime(p[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                    rows.append((ts, float(p[2]), float(p[3]), p[6:10],
+                                 float(p[4]) if p[4] not in ("[N/A]", "") else 0.0))
                 except ValueError:
                     continue
         os.unlink(self.path)
         if not rows:
             return None
+        inside = [r for r in rows if self.window and self.window[0] <= r[0] <= self.window[1]]
+        if inside:
+            use = inside
+        else:  # a region shorter than the sampling period: the samples nearest to it
+            mid = (self.window[0] + self.window[1]) / 2 if self.window else rows[-1][0]
+            use = sorted(rows, key=lambda r: abs(r[0] - mid))[:2]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[2]) if v.lower() == "active"})
-        loaded = [r for r in rows if r[3] > 200.0] or rows
-        return {"sm_mhz": statistics.median(r[0] for r in loaded), "sm_max_mhz": max(r[1] for r in rows),
-                "reasons": reasons, "samples": len(rows)}
+        reasons = sorted({names[i] for r in use for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[1] for r in use), "sm_max_mhz": max(r[2] for r in use),
+                "reasons": reasons, "samples": len(use), "samples_in_region": len(inside),
+                "sample_ms": self.SAMPLE_MS}
 
 
 def cpu_sample_gflops(A_rows, B, cpg=4, target_s=1.0, max_runs=20):
@@ -352,11 +369,13 @@ def run_ours(args, rank, world, local, pg):
     torch.cuda.synchronize()
     launches0 = L.gcoo_kernel_launches()
     with Clocks(local) as clk:
+        t_region = time.time()
         e0.record(stream)
         for _ in range(args.steps):
             h.multiply_by(B, Cd)
         e1.record(stream)
         torch.cuda.synchronize()
+        clk.mark(t_region, time.time())
     launches = L.gcoo_kernel_launches() - launches0
     barrier(pg)
     ms = max_over_ranks(pg, e0.elapsed_time(e1) / args.steps)
