@@ -14,6 +14,7 @@ operand, given dense), B is k x n, C = A @ B is m x n.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from typing import Optional
 
 from ._native import (  # noqa: F401
@@ -112,6 +113,17 @@ class GcooHandle:
                                     C.byref(p)))
         self.rows_per_group = rows_per_group
         return self
+
+    @classmethod
+    def from_matrix_market(cls, path: str, rows_per_group: int = 4, **params) -> "GcooHandle":
+        """Handle for the matrix of a Matrix Market file (the reference
+        driver's -file= input), through COO triplets on the current CUDA
+        device; see read_matrix_market for the file semantics."""
+        torch = _torch()
+        rows, cols, vals, m, k = read_matrix_market(path)
+        dev = torch.device("cuda")
+        return cls.from_coo(torch.from_numpy(rows).to(dev), torch.from_numpy(cols).to(dev),
+                            torch.from_numpy(vals).to(dev), m, k, rows_per_group, **params)
 
     @property
     def ptr(self):
@@ -227,6 +239,29 @@ class GcooHandle:
         check(lib().gcoo_autotune(self._h, C.c_void_p(B.data_ptr()), n, C.c_void_p(Cout.data_ptr()),
                                   _stream_ptr(stream), C.byref(p)))
         return {"vec": p.vec, "warps": p.warps, "col_warps": p.col_warps}
+
+
+def read_matrix_market(path: str):
+    """A Matrix Market coordinate file as (rows, cols, vals, m, k): int32,
+    int32 and float32 NumPy arrays of 0-based triplets in file order, each
+    mirror (symmetric, skew-symmetric) right after its entry; pattern
+    entries are 1.0. Host code only (gcoo_read_matrix_market)."""
+    import numpy as np
+    m, k, n = C.c_int64(), C.c_int64(), C.c_int64()
+    r, c = C.POINTER(C.c_int32)(), C.POINTER(C.c_int32)()
+    v = C.POINTER(C.c_float)()
+    L = lib()
+    check(L.gcoo_read_matrix_market(os.fsencode(path), C.byref(m), C.byref(k), C.byref(n), C.byref(r),
+                                    C.byref(c), C.byref(v)))
+    try:
+        cnt = int(n.value)
+        rows = np.ctypeslib.as_array(r, shape=(max(cnt, 1),))[:cnt].copy()
+        cols = np.ctypeslib.as_array(c, shape=(max(cnt, 1),))[:cnt].copy()
+        vals = np.ctypeslib.as_array(v, shape=(max(cnt, 1),))[:cnt].copy()
+    finally:
+        for ptr in (r, c, v):
+            L.gcoo_free_host(C.cast(ptr, C.c_void_p))
+    return rows, cols, vals, int(m.value), int(k.value)
 
 
 def convert_count(A, rows_per_group=4, stream=None):

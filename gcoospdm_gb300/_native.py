@@ -36,6 +36,7 @@ EXPORTS = (
     "gcoo_batch_create", "gcoo_batch_run", "gcoo_batch_launches", "gcoo_batch_destroy",
     "gcoo_session_create", "gcoo_session_multiply", "gcoo_session_stats", "gcoo_session_destroy",
     "gcoo_autotune", "gcoo_autotune_save", "gcoo_autotune_load", "gcoo_autotune_clear",
+    "gcoo_read_matrix_market", "gcoo_free_host",
 )
 
 
@@ -121,6 +122,10 @@ def _declare(L) -> None:
         "gcoo_autotune_save": (st, [C.c_char_p]),
         "gcoo_autotune_load": (st, [C.c_char_p]),
         "gcoo_autotune_clear": (st, []),
+        "gcoo_read_matrix_market": (st, [C.c_char_p, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
+                                         C.POINTER(C.POINTER(i32)), C.POINTER(C.POINTER(i32)),
+                                         C.POINTER(C.POINTER(C.c_float))]),
+        "gcoo_free_host": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -86,6 +86,7 @@ int main(int argc, char **argv)
         printf("Usage -nRowsA=nRowsA -nColsA=nColsA -nRowsB=nRowsB -nColsB=nColsB\n"
                "      -sparsity=sparsity (of matrix B) -algo=gcoospdm|cublas|cusparse|csr\n"
                "      -kernelonly=0|1 -seed=N -check=0|1 -prec=fp32|bf16|split|fp8 -reps=N\n"
+               "      -file=matrix.mtx (Matrix Market; then C = M x M for the file's square M)\n"
                "nColsB should equal nRowsA\n");
         return 0;
     }
@@ -104,22 +105,46 @@ int main(int argc, char **argv)
     bool check = geti("check", 0) == 1;
     const char *pv = flag_value(argc, argv, "prec");
     std::string prec = pv ? pv : "fp32";
-    if (flag_value(argc, argv, "file")) {
-        fprintf(stderr, "-file (Matrix Market input) is not supported by this driver\n");
-        return 2;
-    }
-    if (nColsB != nRowsA) {
-        fprintf(stderr, "nColsB (%zu) must equal nRowsA (%zu)\n", nColsB, nRowsA);
-        return 2;
-    }
     gcoo_precision gp = GCOO_PREC_FP32;
     if (prec == "bf16") gp = GCOO_PREC_BF16;
     else if (prec == "split") gp = GCOO_PREC_SPLIT_BF16;
     else if (prec == "fp8") gp = GCOO_PREC_FP8_B;
 
     std::vector<float> A, B;
-    fill(A, nRowsA, nColsA, seed, 1.0, false);
-    long long nnz = fill(B, nRowsB, nColsB, seed, 1.0 - sparsity, true);
+    long long nnz = 0;
+    const char *file = flag_value(argc, argv, "file");
+    if (file) {
+        // C = M x M for the file's matrix M (src/main.cu:149-176): M is the
+        // sparse operand and, densified, the dense one too
+        int64_t fm = 0, fk = 0, cnt = 0;
+        int32_t *fr = nullptr, *fc = nullptr;
+        float *fv = nullptr;
+        if (!*file || gcoo_read_matrix_market(file, &fm, &fk, &cnt, &fr, &fc, &fv) != GCOO_SUCCESS) {
+            fprintf(stderr, "-file: %s\n", *file ? gcoo_last_error() : "no file name");
+            return 2;
+        }
+        printf("Read mtx file: %s\n", file);
+        if (fm != fk) {
+            fprintf(stderr, "-file: C = M x M needs a square matrix, got %lld x %lld\n", (long long)fm, (long long)fk);
+            gcoo_free_host(fr), gcoo_free_host(fc), gcoo_free_host(fv);
+            return 2;
+        }
+        B.assign(static_cast<size_t>(fm) * static_cast<size_t>(fk), 0.0f);
+        for (int64_t i = 0; i < cnt; ++i) // in file order: a later duplicate overwrites, as in the reference
+            B[static_cast<size_t>(fr[i]) * static_cast<size_t>(fk) + static_cast<size_t>(fc[i])] = fv[i];
+        gcoo_free_host(fr), gcoo_free_host(fc), gcoo_free_host(fv);
+        A = B;
+        nRowsA = nColsA = nRowsB = nColsB = static_cast<size_t>(fm);
+        for (float x : B)
+            nnz += x != 0.0f;
+    } else {
+        if (nColsB != nRowsA) {
+            fprintf(stderr, "nColsB (%zu) must equal nRowsA (%zu)\n", nColsB, nRowsA);
+            return 2;
+        }
+        fill(A, nRowsA, nColsA, seed, 1.0, false);
+        nnz = fill(B, nRowsB, nColsB, seed, 1.0 - sparsity, true);
+    }
     printf("nnz cpu: %lld, density: %.4f\n", nnz, nnz * 1.0 / (double)(nRowsB * nColsB));
     printf("A[%zu,%zu] * B[%zu,%zu]\n", nRowsA, nColsA, nRowsB, nColsB);
     printf("Algorithm: %s\n", algo.c_str());

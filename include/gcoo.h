@@ -133,6 +133,23 @@ gcoo_status gcoo_create_coo(gcoo_handle **out, int64_t m, int64_t k, const int32
                             const int32_t *d_cols, const float *d_vals, int64_t nnz,
                             const gcoo_params *params);
 
+/* The reference driver's -file= input (src/MatrixReader.cpp:11-84): a
+ * Matrix Market file read on the host into COO triplets for
+ * gcoo_create_coo (copied to the device by the caller), without a dense
+ * m x k buffer. Coordinate format; real, integer or pattern values;
+ * general, symmetric or skew-symmetric. Indices become 0-based; triplets
+ * keep the file's order with each mirror right after its entry, so a later
+ * duplicate wins as in the reference's dense buffer. Pattern entries are
+ * 1.0 (the reference draws unseeded rand() values) and a skew-symmetric
+ * mirror is negated (the reference copies it unchanged). The three arrays
+ * are allocated here; release each with gcoo_free_host. Errors:
+ * GCOO_ERROR_INVALID_VALUE for a missing, malformed or truncated file or an
+ * index out of range, GCOO_ERROR_UNSUPPORTED for the array format, complex
+ * values or hermitian symmetry, GCOO_ERROR_FORMAT beyond int32. */
+gcoo_status gcoo_read_matrix_market(const char *path, int64_t *m, int64_t *k, int64_t *count,
+                                    int32_t **rows, int32_t **cols, float **vals);
+void gcoo_free_host(void *p);
+
 /* build() (src/ShGCOOSpDM.cu:182-193): dense -> GCOO conversion into
  * handle-owned arrays (count, device exclusive scan, stable scatter). Reads
  * the total nnz back to size the arrays, so it synchronises `stream` once

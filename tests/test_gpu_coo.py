@@ -96,3 +96,36 @@ def test_coo_zipf_matches_dense_build(native, torch):
         assert torch.equal(ac[f], ad[f]), f
     B = dg.dense_pm1_torch(5, 5, k, 256, device="cuda")
     assert torch.equal(hc.spdm(B), hd.spdm(B))
+
+
+def test_matrix_market_file_through_the_handle_and_the_driver(native, oracle_mod, torch, tmp_path):
+    """The reference driver's -file= input: C = M x M for the matrix M of a
+    Matrix Market file (symmetric, lower triangle stored, with duplicates
+    and explicit zeros). GcooHandle.from_matrix_market gives the oracle's
+    bits on the densified M; `gcoo_main -file= -check=1` passes its FP64
+    check."""
+    import os
+    import subprocess
+    n, e = 300, 2500
+    rng = np.random.default_rng(61)
+    r = rng.integers(1, n + 1, size=e)
+    c = rng.integers(1, n + 1, size=e)
+    r, c = np.maximum(r, c), np.minimum(r, c)
+    v = rng.uniform(-1.0, 1.0, size=e).astype(np.float32)
+    v[::17] = 0.0
+    path = tmp_path / "sym.mtx"
+    path.write_text("%%MatrixMarket matrix coordinate real symmetric\n% test matrix\n"
+                    f"{n} {n} {e}\n" + "".join(f"{a} {b} {x:.9g}\n" for a, b, x in zip(r, c, v)))
+    rows, cols, vals, m, k = native.read_matrix_market(str(path))
+    M = densify(m, k, rows, cols, vals)
+    assert np.array_equal(M, M.T)
+    h = native.GcooHandle.from_matrix_market(str(path)).build()
+    assert h.nnz == int(np.count_nonzero(M))
+    got = h.spdm(torch.from_numpy(M).cuda()).cpu().numpy()
+    ref = oracle_mod.spdm(oracle_mod.convert(M), M)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+    main = os.path.join(os.path.dirname(native.__file__), "_build", "gcoo_main")
+    out = subprocess.run([main, f"-file={path}", "-algo=gcoospdm", "-check=1", "-reps=3"],
+                         capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "Read mtx file" in out.stdout and "Test passed" in out.stdout and "Time:" in out.stdout
