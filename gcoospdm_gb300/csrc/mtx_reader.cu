@@ -115,7 +115,8 @@ gcoo_status gcoo_read_matrix_market(const char *path, int64_t *m, int64_t *k, in
 
     std::vector<int32_t> r, c;
     std::vector<float> v;
-    const size_t want = static_cast<size_t>(std::min<long long>(ne, 1LL << 26)) * (mirror ? 2 : 1);
+    // reserved from the size line, but not trusting it beyond 4 M entries (the vectors grow past that)
+    const size_t want = static_cast<size_t>(std::min<long long>(ne, 1LL << 22)) * (mirror ? 2 : 1);
     r.reserve(want);
     c.reserve(want);
     v.reserve(want);
