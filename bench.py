@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--no-gpu-baselines", action="store_true",
                     help="skip timing the reference algorithm, cuSPARSE and cuBLAS on the same GPU")
     ap.add_argument("--sweep", action="store_true", help="print the FP32 n x sparsity sweep instead")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the sweep key of the main line")
     ap.add_argument("--case", choices=["tc_bf16", "tc_split", "convert", "fp32", "batched", "fp8", "bf16_fma",
                                        "fp32_block", "convert_irregular", "spdm_irregular"],
                     help="run one small case a few times (for profiling) and exit")
@@ -214,6 +215,18 @@ class Clocks:
                 "sample_ms": self.SAMPLE_MS}
 
 
+def workload_config(n: int, sparsity: float, nnz: int, world: int) -> dict:
+    """The bench line's config, key for key the same in both arms: the square
+    FP32 workload (A n x n Bernoulli(1 - sparsity), B n x n), its nonzeros and
+    the GPU arm's timing hygiene (no L2 flush: A and B each exceed L2)."""
+    p = 1.0 - sparsity
+    mb = 4 * n * n / 1e6
+    return {"workload": f"fp32 gcoo convert+multiply, A {n}x{n} bernoulli p={p:g} U(-1,1), B {n}x{n} U(-1,1)",
+            "m": n, "k": n, "n": n, "sparsity": sparsity, "nnz": int(nnz), "rows_per_group": 4,
+            "l2": f"no flush: inputs larger than L2 (A and B {mb:.0f} MB each, L2 129 MB)",
+            "parallelism": f"replicas x{world}"}
+
+
 def cpu_sample_gflops(A_rows, B, cpg=4, target_s=1.0, max_runs=20):
     """Oracle port (convert + multiply) on a row sample, all host threads:
     repeated for about target_s seconds (at least 3, at most max_runs runs)."""
@@ -262,9 +275,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded splitmix64)",
-        "config": {"workload": f"fp32 gcoo convert+multiply, A {n}x{n} bernoulli p={p:g} U(-1,1), B {n}x{n} U(-1,1)",
-                   "m": n, "k": n, "n": n, "sparsity": args.sparsity, "rows_per_group": 4,
-                   "l2": "host run (no GPU)"},
+        "config": workload_config(n, args.sparsity, dg.bernoulli_nnz(SEED, n, n, p), world),
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": nt, "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference has no CPU implementation of this path; the oracle restates its algorithm "
@@ -397,6 +408,9 @@ def run_ours(args, rank, world, local, pg):
     alg_bytes = 12 * nnz + 8 * (ng + 1) + 4 * k * n + 4 * m * n
     peaks, peak_kind = measured_peaks()
     achieved = alg_bytes / t_spdm / 1e9
+    # the L2 -> SM read peak, measured live on this GPU (512-byte gathers from an L2-resident region)
+    l2_peak = g.measure_l2_read_gbs()
+    l2_bytes = 4.0 * nnz * n  # the B rows the multiply gathers: n floats per entry
     prof = load_profile_traffic()
     traffic = None
     if prof and prof.get("n") == n and abs(prof.get("sparsity", 0) - args.sparsity) < 1e-9:
@@ -483,6 +497,18 @@ def run_ours(args, rank, world, local, pg):
     if not args.no_forms:
         forms = run_forms(args, g, dg, torch, dev)
 
+    sweep = None
+    if rank == 0 and world == 1 and not args.no_sweep:
+        try:
+            sweep = {"note": "multiply alone (FP32), square A n x n Bernoulli, B n x n, timed as CUDA-graph "
+                             "replays of back-to-back calls; hbm_frac of the measured copy peak, l2_frac of the "
+                             "live L2 read peak; B fits L2 for n <= 4096",
+                     "l2_peak_gbs": round(l2_peak, 1),
+                     "points": sweep_points(g, dg, torch, dev, peaks, l2_peak)}
+        except Exception as e:  # the main line still prints
+            sweep = {"error": f"{type(e).__name__}: {e}"}
+        torch.cuda.empty_cache()
+
     gpu_baselines = None
     if rank == 0 and world == 1 and not args.no_gpu_baselines:
         gpu_baselines = run_gpu_baselines(g, torch, A, B, flop)
@@ -494,14 +520,15 @@ def run_ours(args, rank, world, local, pg):
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": round(value / 117.1, 3) if (n == 8192 and abs(args.sparsity - 0.99) < 1e-9) else None,
         "dtype": "f32", "data": "synthetic (seeded splitmix64; U(-1,1) values, Bernoulli mask)",
-        "config": {"workload": f"fp32 gcoo convert+multiply, A {m}x{k} bernoulli p={p:g} U(-1,1), B {k}x{n} U(-1,1)",
-                   "m": m, "k": k, "n": n, "sparsity": args.sparsity, "nnz": nnz, "rows_per_group": 4,
-                   "l2": "no flush: inputs larger than L2 (A and B 268 MB each, L2 129 MB)",
-                   "parallelism": f"replicas x{world}"},
+        "config": workload_config(n, args.sparsity, nnz, world),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic,
                      "kernel": "spdm_fp32_kernel", "algorithmic_bytes": alg_bytes,
-                     "kernel_ms": round(t_spdm * 1e3, 4), "peak_source": peak_kind},
+                     "kernel_ms": round(t_spdm * 1e3, 4), "peak_source": peak_kind,
+                     "l2_read_bytes": int(l2_bytes), "l2_achieved_gbs": round(l2_bytes / t_spdm / 1e9, 1),
+                     "l2_peak_gbs": round(l2_peak, 1), "l2_peak_source": "measured live (bench.py)",
+                     "l2_frac": round(l2_bytes / t_spdm / 1e9 / l2_peak, 4) if l2_peak else None,
+                     "binding": "l2" if l2_peak and l2_bytes / l2_peak > alg_bytes / peaks["hbm_gbs"] else "hbm"},
         "l2_path": l2_path,
         "fma_roofline": {"achieved_tflops": round(flop / t_spdm / 1e12, 3), "nominal_peak_tflops": round(fma_peak, 1),
                          "frac": round(flop / t_spdm / 1e12 / fma_peak, 4)},
@@ -517,6 +544,8 @@ def run_ours(args, rank, world, local, pg):
         line["gpu_baselines"] = gpu_baselines
     if forms:
         line["forms"] = forms
+    if sweep:
+        line["sweep"] = sweep
     print(json.dumps(line), flush=True)
 
 
@@ -532,6 +561,29 @@ def _time(torch, fn, reps=5, warm=2):
     e1.record(stream)
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / reps  # ms
+
+
+def _time_graph(torch, fn, per_graph=10, replays=3):
+    """Device time per call of fn, from a CUDA graph holding per_graph calls
+    (replayed `replays` times after one warm replay): no host launch gaps
+    between calls, which dominate kernels of a few tens of microseconds."""
+    fn()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        for _ in range(per_graph):
+            fn()
+    graph.replay()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(replays):
+        graph.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    del graph
+    return e0.elapsed_time(e1) / (replays * per_graph)  # ms
 
 
 def _rel_fro_rows(torch, A, B, C, rows):
@@ -691,34 +743,54 @@ def run_forms(args, g, dg, torch, dev):
     return out
 
 
-def run_sweep(args):
-    """The FP32 sweep (n x sparsity grid): one JSON line per point."""
-    import torch
-    import gcoospdm_gb300 as g
-    from gcoospdm_gb300 import datagen as dg
-    dev = torch.device("cuda", 0)
-    peaks, _ = measured_peaks()
+def sweep_points(g, dg, torch, dev, peaks, l2_peak, full=False):
+    """The FP32 sweep (n x sparsity grid, square A Bernoulli, B n x n): the
+    multiply alone per point, with its HBM fraction (algorithmic bytes
+    12 nnz + 8 (nGroup + 1) + 8 n^2) and L2 fraction (the B rows gathered,
+    nnz * n * 4 bytes, against the live L2 read peak). full=True adds the
+    conversion, mutiplyBy and (n <= 4096) the error against FP64."""
+    out = []
     for n in (2048, 4096, 8192, 16384):
         B = dg.dense_pm1_torch(n, 5, n, n, device=dev)
         Cd = torch.empty(n, n, device=dev)
         for s in (0.95, 0.98, 0.99, 0.995, 0.999):
             A = dg.bernoulli_dense_torch(n + int(s * 1e4), n, n, 1.0 - s, device=dev)
             h = g.GcooHandle(A)
-            conv = _time(torch, h.build, reps=3, warm=1)
-            ms = _time(torch, lambda: h.spdm(B, Cd), reps=5)
-            e2e = _time(torch, lambda: h.multiply_by(B, Cd), reps=3)
+            conv = _time(torch, h.build, reps=3, warm=1) if full else None
+            if not full:
+                h.build()
+            ms = _time_graph(torch, lambda: h.spdm(B, Cd), per_graph=10 if n <= 8192 else 3)
             nnz = h.nnz
             alg = 12 * nnz + 8 * (n // 4 + 1) + 8 * n * n
-            print(json.dumps({"n": n, "sparsity": s, "nnz": nnz, "convert_ms": round(conv, 4),
-                              "spdm_ms": round(ms, 4), "spdm_gflops": round(2.0 * nnz * n / ms / 1e6, 1),
-                              "spdm_gbps": round(alg / ms / 1e6, 1),
-                              "hbm_frac": round(alg / ms / 1e6 / peaks["hbm_gbs"], 4),
-                              "l2_read_gbps": round(4.0 * nnz * n / ms / 1e6, 1), "multiply_by_ms": round(e2e, 4),
-                              "multiply_by_gflops": round(2.0 * nnz * n / e2e / 1e6, 1),
-                              "rel_fro_vs_fp64": h.error_norm(B, Cd) if n <= 4096 else None}), flush=True)
+            l2b = 4.0 * nnz * n
+            pt = {"n": n, "sparsity": s, "nnz": nnz, "spdm_ms": round(ms, 4),
+                  "spdm_gflops": round(2.0 * nnz * n / ms / 1e6, 1),
+                  "hbm_frac": round(alg / ms / 1e6 / peaks["hbm_gbs"], 4),
+                  "l2_read_gbps": round(l2b / ms / 1e6, 1),
+                  "l2_frac": round(l2b / ms / 1e6 / l2_peak, 4) if l2_peak else None}
+            pt["binding"] = "l2" if (pt["l2_frac"] or 0) >= pt["hbm_frac"] else "hbm"
+            if full:
+                e2e = _time(torch, lambda: h.multiply_by(B, Cd), reps=3)
+                pt.update({"convert_ms": round(conv, 4), "multiply_by_ms": round(e2e, 4),
+                           "multiply_by_gflops": round(2.0 * nnz * n / e2e / 1e6, 1),
+                           "rel_fro_vs_fp64": h.error_norm(B, Cd) if n <= 4096 else None})
+            out.append(pt)
             del A, h
         del B, Cd
         torch.cuda.empty_cache()
+    return out
+
+
+def run_sweep(args):
+    """The FP32 sweep, one JSON line per point."""
+    import torch
+    import gcoospdm_gb300 as g
+    from gcoospdm_gb300 import datagen as dg
+    dev = torch.device("cuda", 0)
+    peaks, _ = measured_peaks()
+    l2_peak = g.measure_l2_read_gbs()
+    for pt in sweep_points(g, dg, torch, dev, peaks, l2_peak, full=True):
+        print(json.dumps({**pt, "l2_peak_gbs": round(l2_peak, 1)}), flush=True)
 
 
 def main():

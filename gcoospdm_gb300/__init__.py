@@ -506,6 +506,8 @@ class _BaselineGemm(ShGemm):
             L.gcoo_refalgo_build.restype = C.c_int
             L.gcoo_refalgo_build.argtypes = [C.c_void_p]
             L.gcoo_refalgo_destroy.argtypes = [C.c_void_p]
+            L.gcoo_measure_l2_read_gbs.restype = C.c_double
+            L.gcoo_measure_l2_read_gbs.argtypes = [C.c_int]
             cls._L = L
         return cls._L
 
@@ -532,6 +534,13 @@ class _BaselineGemm(ShGemm):
                 self._lib().gcoo_baseline_destroy(self._g)
         except Exception:
             pass
+
+
+def measure_l2_read_gbs(reps: int = 3) -> float:
+    """The L2 -> SM read peak of the current GPU in GB/s: 512-byte warp-wide
+    loads at random offsets of an L2-resident 32 MB region (the shape of the
+    multiply's B-row loads), best of `reps` launches. 0.0 on a CUDA error."""
+    return float(_BaselineGemm._lib().gcoo_measure_l2_read_gbs(int(reps)))
 
 
 class RefAlgoBaseline:

@@ -18,13 +18,20 @@
 // Set-up: host code cannot use the array's name as a device address (on the
 // host it names a host-side shadow), so the first call on each device, with
 // that device current, looks the address up once with cudaGetSymbolAddress
-// and caches it per device. Make that first call outside any stream capture.
+// and caches it per device, together with the id of the CUDA context it was
+// found in. A later call in another context on that device (after
+// cudaDeviceReset, or once the primary context was released and created
+// again, when the module is loaded anew and the array may move) looks it up
+// again. Make the first call on a device, and the first after such a reset,
+// outside any stream capture.
 //
 // Sharing: all calls on a device use the same array, and it keeps whatever
 // the previous call left. Nothing in it has to start at zero -- each call
 // writes every count and every block sum before reading it -- but calls
 // whose kernels overlap on the GPU (different streams, no ordering) race on
 // the array: order them, or use gcoo_convert_count.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "internal.cuh"
@@ -42,7 +49,40 @@ static __device__ __align__(256) unsigned char g_count_scratch[kStaticScratchByt
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-unsigned char *g_scratch[kMaxDevices] = {};
+struct ScratchAddr {
+    unsigned char *ptr = nullptr;
+    unsigned long long ctx_id = 0; // context the address was looked up in (0: unknown)
+};
+ScratchAddr g_scratch[kMaxDevices];
+
+// Unique id of the calling thread's current CUDA context, 0 when there is none
+// or the driver cannot say (the address is then looked up on every call).
+// The driver functions come through the runtime's entry-point query, so the
+// library links no driver library.
+unsigned long long current_context_id()
+{
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void *f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 
 gcoo_status scratch_for_current_device(unsigned char **out)
 {
@@ -53,14 +93,17 @@ gcoo_status scratch_for_current_device(unsigned char **out)
     if (dev < 0 || dev >= kMaxDevices)
         return fail(GCOO_ERROR_UNSUPPORTED, "device ordinal beyond the static scratch table");
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch[dev]) {
+    ScratchAddr &c = g_scratch[dev];
+    const unsigned long long id = current_context_id();
+    if (!c.ptr || id == 0 || id != c.ctx_id) {
         void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_count_scratch);
+        e = cudaGetSymbolAddress(&p, g_count_scratch); // loads the module into the current context if needed
         if (e != cudaSuccess || !p)
             return cuda_fail(e != cudaSuccess ? e : cudaErrorInvalidSymbol, "cudaGetSymbolAddress(g_count_scratch)");
-        g_scratch[dev] = static_cast<unsigned char *>(p);
+        c.ptr = static_cast<unsigned char *>(p);
+        c.ctx_id = current_context_id(); // the context exists now, if it did not before
     }
-    *out = g_scratch[dev];
+    *out = c.ptr;
     return GCOO_SUCCESS;
 }
 

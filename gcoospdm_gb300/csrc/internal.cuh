@@ -159,6 +159,7 @@ struct LaunchShape {
     int depth;     // 1: plain batches, 2: B loads of the next batch in flight
     int rows;      // rows per CTA
     int col_iters = 1; // column tiles each warp walks with one staging of its group's entries
+    int chunk = 0;     // entries staged per pass (shared memory), 0: the full 2048
 };
 // Heavy-tailed row lengths: the longest row at least 256 entries and above 8x the mean.
 bool row_lengths_skewed(int64_t m, int64_t nnz, int64_t max_row);

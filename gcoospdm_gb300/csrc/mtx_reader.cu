@@ -10,6 +10,13 @@
 // Differences, both where the reference's values are not the matrix's:
 // pattern entries are 1.0 (the reference draws unseeded rand() values), and
 // the mirror of a skew-symmetric entry is negated, as the format defines.
+// "hermitian" is read like "symmetric": for the real, integer and pattern
+// fields read here the conjugate of a value is the value itself (the
+// reference mirrors every banner that does not say "general").
+//
+// No C++ exception leaves the entry point: a host allocation that fails
+// while the triplets grow returns GCOO_ERROR_ALLOC, anything else thrown
+// GCOO_ERROR_INVALID_VALUE.
 #include <errno.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -17,6 +24,7 @@
 
 #include <algorithm>
 #include <cctype>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -52,22 +60,10 @@ struct FileCloser {
     }
 };
 
-} // namespace
-} // namespace gcoo
-
-using namespace gcoo;
-
-extern "C" {
-
-gcoo_status gcoo_read_matrix_market(const char *path, int64_t *m, int64_t *k, int64_t *count, int32_t **rows,
-                                    int32_t **cols, float **vals)
+// The reader proper; its std::vector / std::string work may throw.
+gcoo_status read_matrix_market(const char *path, int64_t *m, int64_t *k, int64_t *count, int32_t **rows,
+                               int32_t **cols, float **vals)
 {
-    if (!path || !m || !k || !count || !rows || !cols || !vals)
-        return fail(GCOO_ERROR_INVALID_VALUE, "NULL argument");
-    *rows = nullptr;
-    *cols = nullptr;
-    *vals = nullptr;
-    *m = *k = *count = 0;
     FileCloser fc{fopen(path, "r")};
     if (!fc.f)
         return fail(GCOO_ERROR_INVALID_VALUE, std::string("cannot open ") + path + ": " + strerror(errno));
@@ -86,6 +82,8 @@ gcoo_status gcoo_read_matrix_market(const char *path, int64_t *m, int64_t *k, in
         return fail(GCOO_ERROR_UNSUPPORTED, "field " + field + " is not read (real, integer or pattern)");
     int mirror = 0; // 0 general, 1 symmetric, -1 skew-symmetric
     if (symmetry == "symmetric")
+        mirror = 1;
+    else if (symmetry == "hermitian") // real-valued fields: the same as symmetric
         mirror = 1;
     else if (symmetry == "skew-symmetric")
         mirror = -1;
@@ -186,6 +184,42 @@ gcoo_status gcoo_read_matrix_market(const char *path, int64_t *m, int64_t *k, in
     *k = nc;
     *count = static_cast<int64_t>(n);
     return GCOO_SUCCESS;
+}
+
+// fail() builds its message in a std::string: if even that cannot be
+// allocated, the status alone is returned.
+gcoo_status fail_nothrow(gcoo_status s, const char *msg) noexcept
+{
+    try {
+        return fail(s, msg);
+    } catch (...) {
+        return s;
+    }
+}
+
+} // namespace
+} // namespace gcoo
+
+using namespace gcoo;
+
+extern "C" {
+
+gcoo_status gcoo_read_matrix_market(const char *path, int64_t *m, int64_t *k, int64_t *count, int32_t **rows,
+                                    int32_t **cols, float **vals)
+{
+    if (!path || !m || !k || !count || !rows || !cols || !vals)
+        return fail(GCOO_ERROR_INVALID_VALUE, "NULL argument");
+    *rows = nullptr;
+    *cols = nullptr;
+    *vals = nullptr;
+    *m = *k = *count = 0;
+    try {
+        return read_matrix_market(path, m, k, count, rows, cols, vals);
+    } catch (const std::bad_alloc &) {
+        return fail_nothrow(GCOO_ERROR_ALLOC, "host allocation failed while reading the file");
+    } catch (...) {
+        return fail_nothrow(GCOO_ERROR_INVALID_VALUE, "the file could not be read");
+    }
 }
 
 void gcoo_free_host(void *p) { free(p); }

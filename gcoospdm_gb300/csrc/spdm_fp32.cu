@@ -21,8 +21,7 @@ namespace gcoo {
 
 namespace {
 
-constexpr int kChunk = 2048; // entries staged per pass (16 KB)
-constexpr int kSmemBytes = 128 + (kChunk + 2) * static_cast<int>(sizeof(Entry));
+constexpr int kChunk = 2048; // most entries staged per pass (16 KB)
 
 template <int V>
 struct Vec;
@@ -176,7 +175,7 @@ template <int V, int MAXT, bool PIPE, bool MULTI>
 __global__ void __launch_bounds__(MAXT)
 spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ row_ptr, int64_t m,
                  int32_t cpg, const float *__restrict__ B, int64_t n, float *__restrict__ C,
-                 int32_t col_warps, int32_t col_iters, uint32_t *__restrict__ status)
+                 int32_t col_warps, int32_t col_iters, int32_t chunk_cap, uint32_t *__restrict__ status)
 {
     if (!MULTI)
         col_iters = 1;
@@ -193,7 +192,6 @@ spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ r
     const int64_t tile_stride = static_cast<int64_t>(col_warps) * (32 * V);
     const int64_t j = (static_cast<int64_t>(blockIdx.y) * col_iters * col_warps + sub) * (32 * V) +
                       static_cast<int64_t>(lane) * V;
-    const bool has_col = j < n;
 
     const int64_t gs = row_ptr[r0];
     const int64_t ge = row_ptr[r_end];
@@ -209,47 +207,58 @@ spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ r
     __syncthreads();
 
     float acc[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v)
-        acc[v] = 0.0f;
-    const float *Bj = B + j;
-
+    // chunk: entries staged per pass, what the launch's shared memory holds
+    const int64_t chunk = chunk_cap < kChunk ? chunk_cap : kChunk;
     const int64_t total = ge - gs;
-    const int64_t nchunks = (total + kChunk - 1) / kChunk;
+    const int64_t nchunks = (total + chunk - 1) / chunk;
+    // several column tiles per warp from one staging (the group fits one
+    // chunk): every tile, the first included, is walked after the staging,
+    // two at a time for short rows
+    const bool multi_all = MULTI && col_iters > 1 && nchunks == 1;
+    // otherwise each of the warp's tiles walks the group chunk by chunk
+    const int tiles_staged = multi_all ? 1 : col_iters;
     bool ok = true;
-    for (int64_t ch = 0; ch < nchunks && ok; ++ch) {
-        const int64_t cs = gs + ch * kChunk;
-        const int64_t ce = cs + kChunk < ge ? cs + kChunk : ge;
-        const int64_t a0 = cs & ~static_cast<int64_t>(1); // 16-byte aligned superset
-        const int64_t a1 = (ce + 1) & ~static_cast<int64_t>(1);
-        if (threadIdx.x == 0) {
-            fence_proxy_async();
-            const uint32_t bytes = static_cast<uint32_t>((a1 - a0) * static_cast<int64_t>(sizeof(Entry)));
-            mbar_arrive_expect_tx(bar, bytes);
-            bulk_g2s(s_nz, packed + a0, bytes, bar);
+    uint32_t phase = 0;
+    for (int it = 0; it < tiles_staged && ok; ++it) {
+        const int64_t jt = j + it * tile_stride;
+        const float *Bj = B + jt;
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+            acc[v] = 0.0f;
+        for (int64_t ch = 0; ch < nchunks; ++ch, ++phase) {
+            const int64_t cs = gs + ch * chunk;
+            const int64_t ce = cs + chunk < ge ? cs + chunk : ge;
+            const int64_t a0 = cs & ~static_cast<int64_t>(1); // 16-byte aligned superset
+            const int64_t a1 = (ce + 1) & ~static_cast<int64_t>(1);
+            if (threadIdx.x == 0) {
+                fence_proxy_async();
+                const uint32_t bytes = static_cast<uint32_t>((a1 - a0) * static_cast<int64_t>(sizeof(Entry)));
+                mbar_arrive_expect_tx(bar, bytes);
+                bulk_g2s(s_nz, packed + a0, bytes, bar);
+            }
+            const bool waited = mbar_wait(bar, phase & 1);
+            ok = __syncthreads_and(waited) != 0;
+            if (!ok) {
+                if (threadIdx.x == 0)
+                    atomicOr(status, kStatusWaitTimeout);
+                mbar_wait(bar, phase & 1); // let the copy in flight land
+                break;
+            }
+            const int64_t lo = rs > cs ? rs : cs;
+            const int64_t hi = re < ce ? re : ce;
+            if (!multi_all && jt < n && lo < hi)
+                row_chain<V, (MAXT > 512 ? 4 : 8), PIPE>(s_nz + (lo - a0), static_cast<int>(hi - lo), Bj, n, acc);
+            __syncthreads(); // buffer free before the next copy
         }
-        const bool waited = mbar_wait(bar, static_cast<uint32_t>(ch & 1));
-        ok = __syncthreads_and(waited) != 0;
-        if (!ok) {
-            if (threadIdx.x == 0)
-                atomicOr(status, kStatusWaitTimeout);
-            mbar_wait(bar, static_cast<uint32_t>(ch & 1)); // let the copy in flight land
-            break;
-        }
-        const int64_t lo = rs > cs ? rs : cs;
-        const int64_t hi = re < ce ? re : ce;
-        if (has_col && lo < hi)
-            row_chain<V, (MAXT > 512 ? 4 : 8), PIPE>(s_nz + (lo - a0), static_cast<int>(hi - lo), Bj, n, acc);
-        __syncthreads(); // buffer free before the next copy
+        if (!multi_all && has_row && jt < n && ok)
+            Vec<V>::store(C + row * n + jt, acc);
     }
-    if (has_row && has_col && ok)
-        Vec<V>::store(C + row * n + j, acc);
-    // further column tiles of the same rows: the (single) chunk is still staged
-    if (MULTI && col_iters > 1 && nchunks == 1 && ok && has_row) {
+    // all column tiles of the warp's row from the (single) staged chunk
+    if (multi_all && ok && has_row) {
         const int64_t a0 = gs & ~static_cast<int64_t>(1);
         const Entry *s_row = s_nz + (rs - a0);
         const int cnt = static_cast<int>(re - rs);
-        int it = 1;
+        int it = 0;
         // very short rows: two tiles at a time, twice the B loads in flight
         // (longer rows already keep a batch of 8 loads in flight per tile)
         for (; cnt < 16 && it + 1 < col_iters; it += 2) {
@@ -440,9 +449,19 @@ LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, 
         v = 1;
     s.vec = v;
     const int cpg = s.rows;
+    // Every group fits one staging chunk: one staging of a group's entries
+    // can serve several column tiles per warp.
+    const bool one_chunk = max_row > 0 && max_row * static_cast<int64_t>(s.rows) + 2 <= kChunk;
     int cw;
     if (p.col_warps > 0)
         cw = p.col_warps;
+    else if (p.warps <= 0 && !skewed && one_chunk)
+        // One warp per row, 4-warp CTAs, each warp walking several column
+        // tiles of its row: measured on GB300 1.06 against 1.15 ms (8192^2,
+        // 1 %) and 0.178 against 0.201 ms (8192^2, 0.1 %) for two warps per
+        // row: twice the CTAs resident per SM keep more B loads in flight,
+        // and the latency of the loads is what bounds these matrices.
+        cw = 1;
     else {
         const int target = p.warps > 0 ? p.warps : 8;
         cw = target / cpg;
@@ -457,20 +476,24 @@ LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, 
     s.col_warps = cw;
     s.warps = cw * cpg;
     s.depth = p.depth > 0 ? p.depth : (skewed ? 2 : 1);
-    // Short rows: one staging of a group's entries serves several column
-    // tiles (about 64 entries per warp), when every group fits one chunk.
     s.col_iters = 1;
-    if (max_row > 0 && max_row * static_cast<int64_t>(s.rows) + 2 <= kChunk) {
+    if (one_chunk) {
         const int64_t tile = static_cast<int64_t>(s.col_warps) * 32 * s.vec;
         const int64_t ny = (n + tile - 1) / tile;
-        const double per_row = mean > 1.0 ? mean : 1.0;
-        int64_t ci = static_cast<int64_t>(64.0 / per_row);
-        // keep about four waves of CTAs (6 resident per SM) for latency hiding
+        // about 768 columns per CTA (0.5-0.9 K columns measured best from
+        // 2048^2 to 16384^2 at 1 % to 0.1 % density), but at least two waves
+        // of CTAs (12 four-warp CTAs resident per SM) on small matrices
+        int64_t ci = 768 / tile;
         const int64_t groups = (m + s.rows - 1) / s.rows;
-        const int64_t by_grid = groups * ny / (static_cast<int64_t>(device_sms()) * 24);
+        const int64_t resident = static_cast<int64_t>(device_sms()) * (s.warps <= 4 ? 12 : 6);
+        const int64_t by_grid = groups * ny / (2 * resident);
         ci = ci > by_grid ? by_grid : ci;
         ci = ci < 1 ? 1 : (ci > ny ? ny : ci);
         s.col_iters = static_cast<int>(ci > 64 ? 64 : ci);
+        // shared memory for the largest possible group only, not a full
+        // chunk: the rest of the SM's L1 array then holds B loads in flight
+        // (measured 2-6 % faster at 0.1-1 % density)
+        s.chunk = static_cast<int>(max_row * s.rows);
     }
     return s;
 }
@@ -488,14 +511,18 @@ cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_
         return cudaErrorInvalidConfiguration;
     dim3 grid(static_cast<unsigned>(ng), static_cast<unsigned>(ny));
     const int threads = s.warps * 32;
+    // entries staged per pass and the shared memory that holds them (the
+    // kernel stages any larger group in several passes)
+    const int chunk = s.chunk > 0 && s.chunk < kChunk ? s.chunk : kChunk;
+    const int smem = 128 + (chunk + 2) * static_cast<int>(sizeof(Entry));
 #define GCOO_FP32_LAUNCH(V, T, P)                                                                       \
     do {                                                                                                \
         if (s.col_iters > 1)                                                                            \
-            spdm_fp32_kernel<V, T, P, true><<<grid, threads, kSmemBytes, st>>>(                         \
-                packed, row_ptr, m, cpg, B, n, C, s.col_warps, s.col_iters, status);                    \
+            spdm_fp32_kernel<V, T, P, true><<<grid, threads, smem, st>>>(                               \
+                packed, row_ptr, m, cpg, B, n, C, s.col_warps, s.col_iters, chunk, status);             \
         else                                                                                            \
-            spdm_fp32_kernel<V, T, P, false><<<grid, threads, kSmemBytes, st>>>(                        \
-                packed, row_ptr, m, cpg, B, n, C, s.col_warps, 1, status);                              \
+            spdm_fp32_kernel<V, T, P, false><<<grid, threads, smem, st>>>(                              \
+                packed, row_ptr, m, cpg, B, n, C, s.col_warps, 1, chunk, status);                       \
     } while (0)
 #define GCOO_FP32_VEC(T, P)                                                                             \
     do {                                                                                                \

@@ -83,6 +83,18 @@ def bernoulli_dense(seed: int, m: int, k: int, p: float, chunk_rows: int = 0) ->
     return out
 
 
+def bernoulli_nnz(seed: int, m: int, k: int, p: float) -> int:
+    """Nonzeros of bernoulli_dense(seed, m, k, p) (the mask alone; values are
+    never zero)."""
+    thr = np.uint64(min(int(p * float(1 << 53)), 1 << 53))
+    step = max(1, (1 << 22) // max(k, 1))
+    total = 0
+    for r0 in range(0, m, step):
+        r1 = min(m, r0 + step)
+        total += int(np.count_nonzero((hash_np(seed, 1, r0 * k, (r1 - r0) * k) >> np.uint64(11)) < thr))
+    return total
+
+
 def dense_pm1(seed: int, stream: int, rows: int, cols: int) -> np.ndarray:
     out = np.empty((rows, cols), dtype=np.float32)
     step = max(1, (1 << 22) // max(cols, 1))

@@ -245,7 +245,9 @@ gcoo_status gcoo_convert_count(const float *dA, int64_t m, int64_t k, int32_t ro
  * it allocates nothing and keeps its per-row counts and block sums in a
  * fixed ~4.2 MB __device__ array held by every GPU that loads the library.
  * Limit: m <= 2^20 rows (larger m -> GCOO_ERROR_INVALID_VALUE). The first
- * call on a device looks up that array's address: make it before any stream
+ * call on a device looks up that array's address and caches it with the
+ * current context's id; the first call after cudaDeviceReset (or in a new
+ * primary context) looks it up again. Make those calls before any stream
  * capture. All calls share the array, so calls that overlap on the GPU race.
  * Synchronises `stream` to return *nnz. */
 gcoo_status gcoo_convert_count_static(const float *dA, int64_t m, int64_t k, int32_t rows_per_group,

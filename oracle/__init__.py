@@ -25,8 +25,13 @@ _ref = None
 
 
 def build() -> None:
-    """Compile the oracle (and the reference emulation where the tree exists)."""
-    subprocess.run(["make", "-s", "-C", _HERE, "-f", "Makefile"], check=True)
+    """Compile the oracle, and the reference kernels (host emulation and
+    sm_103a cubin) when GCOO_REFERENCE_TREE names a reference checkout."""
+    cmd = ["make", "-s", "-C", _HERE, "-f", "Makefile"]
+    tree = os.environ.get("GCOO_REFERENCE_TREE", "")
+    if tree:
+        cmd.append(f"REF={tree}")
+    subprocess.run(cmd, check=True)
 
 
 def lib():

@@ -310,18 +310,21 @@ def test_multiply_by_on_changing_matrices(native, oracle_mod, torch):
 def test_width_beyond_grid_limit_is_refused(native, oracle_mod, torch):
     """Column tiles lie along the grid's y dimension: B wider than 65535
     tiles of the chosen shape is refused with GCOO_ERROR_CUDA before any
-    launch, and the handle stays usable. Rows of 128 entries take one column
-    tile per CTA (short rows walk several, which widens the reach), n odd
-    one column per lane: 64-column tiles."""
+    launch, and the handle stays usable. Groups of 4 rows of 600 entries
+    (more than one staging chunk) take one column tile per CTA (groups that
+    fit one chunk walk several, which widens the reach), n odd one column
+    per lane, two warps per row: 64-column tiles. B (10 GB) is never read."""
     from gcoospdm_gb300 import datagen as dg
     native.autotune_clear()  # the default shape, not a tuned wider one
-    A = dg.bernoulli_dense(42, 8, 128, 1.0)
+    A = dg.bernoulli_dense(42, 8, 600, 1.0)
     h = native.GcooHandle(dev(torch, A), fp32_order="rows").build()
     n = 65535 * 64 + 1
+    wide = torch.empty(600, n, device="cuda")
     with pytest.raises(native.GcooError) as e:
-        h.spdm(torch.ones(128, n, device="cuda"))
+        h.spdm(wide)
     assert e.value.status == 3
-    B = dg.dense_pm1(42, 5, 128, 33)
+    del wide
+    B = dg.dense_pm1(42, 5, 600, 33)
     assert same_bits(h.spdm(dev(torch, B)).cpu().numpy(), oracle_mod.spdm(oracle_mod.convert(A), B))
     assert h.device_status() == 0
 

@@ -107,10 +107,55 @@ def test_pattern_integer_and_skew(native, tmp_path):
     assert rows.size == 0 and (m, k) == (7, 9)
 
 
+def test_hermitian_real_reads_like_symmetric(native, tmp_path):
+    """For real, integer and pattern fields a Hermitian matrix is a symmetric
+    one (the reference mirrors every banner without "general")."""
+    body = "3 3 3\n1 1 2\n3 1 -1.5\n3 2 4\n"
+    herm = native.read_matrix_market(write(tmp_path, "%%MatrixMarket matrix coordinate real hermitian\n" + body, "h.mtx"))
+    sym = native.read_matrix_market(write(tmp_path, "%%MatrixMarket matrix coordinate real symmetric\n" + body, "s.mtx"))
+    for a, b in zip(herm[:3], sym[:3]):
+        assert np.array_equal(a, b)
+    text = "%%MatrixMarket matrix coordinate real hermitian\n" + body
+    assert np.array_equal(dense_from_triplets(*herm), reference_dense(text))
+    rows, cols, vals, _, _ = native.read_matrix_market(
+        write(tmp_path, "%%MatrixMarket matrix coordinate pattern hermitian\n2 2 1\n2 1\n", "hp.mtx"))
+    assert list(zip(rows.tolist(), cols.tolist(), vals.tolist())) == [(1, 0, 1.0), (0, 1, 1.0)]
+
+
+_ALLOC_CHILD = r"""
+import ctypes as C, os, resource, sys
+sys.path.insert(0, sys.argv[1])
+from gcoospdm_gb300 import _native as nat
+L = nat.lib()
+# the library is loaded; now cap the address space a little above what is mapped
+with open("/proc/self/status") as f:
+    vm = next(int(l.split()[1]) for l in f if l.startswith("VmSize:")) * 1024
+resource.setrlimit(resource.RLIMIT_AS, (vm + (40 << 20), resource.RLIM_INFINITY))
+m, k, n = C.c_int64(), C.c_int64(), C.c_int64()
+r, c = C.POINTER(C.c_int32)(), C.POINTER(C.c_int32)()
+v = C.POINTER(C.c_float)()
+st = L.gcoo_read_matrix_market(os.fsencode(sys.argv[2]), C.byref(m), C.byref(k), C.byref(n), C.byref(r),
+                               C.byref(c), C.byref(v))
+print(st, bool(r), L.gcoo_last_error().decode())
+"""
+
+
+def test_host_allocation_failure_returns_a_status(native, tmp_path):
+    """The reader's vectors cannot grow under an address-space limit: the
+    entry point returns GCOO_ERROR_ALLOC (no C++ exception ends the process).
+    A symmetric file whose size line promises 4 M entries makes the reader
+    reserve 3 x 32 MB up front; the child process allows 40 MB more than it
+    has mapped."""
+    p = write(tmp_path, "%%MatrixMarket matrix coordinate real symmetric\n9 9 4194304\n1 1 1\n", "big.mtx")
+    out = subprocess.run(["python", "-c", _ALLOC_CHILD, ROOT, p], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    status, got_rows, msg = out.stdout.split(" ", 2)
+    assert int(status) == 2 and got_rows == "False" and "allocation" in msg
+
+
 @pytest.mark.parametrize("text,status", [
     ("%%MatrixMarket matrix array real general\n2 2\n1\n2\n3\n4\n", 5),
     ("%%MatrixMarket matrix coordinate complex general\n2 2 1\n1 1 1 0\n", 5),
-    ("%%MatrixMarket matrix coordinate real hermitian\n2 2 1\n1 1 1\n", 5),
     ("not a banner\n2 2 1\n1 1 1\n", 1),
     ("%%MatrixMarket matrix coordinate real general\n2 2 1\n3 1 1\n", 1),    # row out of range
     ("%%MatrixMarket matrix coordinate real general\n2 2 1\n0 1 1\n", 1),    # 0 in a 1-based file

@@ -55,6 +55,38 @@ def test_static_count_matches_allocating_entry_point_twice(native, torch):
         assert int(gi[-1]) == nnz and int(npg[-1]) == 0
 
 
+def test_static_count_at_the_row_limit_with_allocation_refused(native, torch):
+    """m = 2^20 exactly (the largest accepted: 256 scan blocks, the total in
+    the array's last slot), run while the library's allocator hook refuses
+    every request: the static entry point still succeeds and never asks."""
+    from gcoospdm_gb300 import _native as nat
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense_torch(303, MAX_ROWS, 4, 0.3, device="cuda")
+    gi_ref, npg_ref, nnz_ref = native.convert_count(A, 4)
+    calls = {"n": 0}
+
+    def alloc(nbytes, ctx):
+        calls["n"] += 1
+        return None
+
+    def release(ptr, ctx):
+        calls["n"] += 1
+
+    L = native.lib()
+    a_cb, f_cb = nat.ALLOC_FN(alloc), nat.FREE_FN(release)
+    assert L.gcoo_set_allocator(a_cb, f_cb, None) == 0
+    try:
+        for _ in range(2):
+            gi, npg, nnz = _static_count(native, torch, A, 4)
+            torch.cuda.synchronize()
+            assert nnz == nnz_ref
+            assert torch.equal(gi, gi_ref)
+            assert torch.equal(npg, npg_ref)
+    finally:
+        assert L.gcoo_set_allocator(nat.ALLOC_FN(0), nat.FREE_FN(0), None) == 0
+    assert calls["n"] == 0
+
+
 def test_static_count_rejects_rows_beyond_limit(native, torch):
     A = torch.zeros(4, 4, device="cuda")
     gi = torch.zeros(8, dtype=torch.int32, device="cuda")
