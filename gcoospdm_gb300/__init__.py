@@ -68,14 +68,17 @@ def _view_tensor(ptr, n, typestr, owner=None):
 
 
 FP32_ORDER = {"auto": 0, "rows": 1, "groups": 2}
+FP32_SUM = {"chain": 0, "split": 1}
 
 
-def make_params(rows_per_group=4, vec=0, warps=0, col_warps=0, engine="auto", depth=0, fp32_order="auto") -> Params:
+def make_params(rows_per_group=4, vec=0, warps=0, col_warps=0, engine="auto", depth=0, fp32_order="auto",
+                fp32_sum="chain") -> Params:
     p = Params()
     check(lib().gcoo_params_default(C.byref(p)))
     p.rows_per_group = rows_per_group
     p.vec, p.warps, p.col_warps, p.depth = vec, warps, col_warps, depth
     p.fp32_order = FP32_ORDER[fp32_order] if isinstance(fp32_order, str) else int(fp32_order)
+    p.fp32_sum = FP32_SUM[fp32_sum] if isinstance(fp32_sum, str) else int(fp32_sum)
     p.engine = ENGINE[engine] if isinstance(engine, str) else int(engine)
     return p
 
@@ -84,14 +87,14 @@ class GcooHandle:
     """One sparse operand: conversion state plus the multiply entry points."""
 
     def __init__(self, A, rows_per_group: int = 4, vec: int = 0, warps: int = 0, col_warps: int = 0,
-                 engine: str = "auto", depth: int = 0, fp32_order: str = "auto"):
+                 engine: str = "auto", depth: int = 0, fp32_order: str = "auto", fp32_sum: str = "chain"):
         _check_f32(A, "A")
         if A.dim() != 2:
             raise ValueError("A must be 2-D")
         self._A = A  # keeps the dense operand alive while the handle may read it
         self.m, self.k = int(A.shape[0]), int(A.shape[1])
         self._h = C.c_void_p()
-        p = make_params(rows_per_group, vec, warps, col_warps, engine, depth, fp32_order)
+        p = make_params(rows_per_group, vec, warps, col_warps, engine, depth, fp32_order, fp32_sum)
         check(lib().gcoo_create(C.byref(self._h), C.c_void_p(A.data_ptr()), self.m, self.k, C.byref(p)))
         self.rows_per_group = rows_per_group
 

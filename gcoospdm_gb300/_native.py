@@ -53,7 +53,7 @@ class GcooError(RuntimeError):
 class Params(C.Structure):
     _fields_ = [("rows_per_group", C.c_int32), ("vec", C.c_int32), ("warps", C.c_int32),
                 ("col_warps", C.c_int32), ("engine", C.c_int32), ("depth", C.c_int32),
-                ("fp32_order", C.c_int32), ("reserved", C.c_int32)]
+                ("fp32_order", C.c_int32), ("fp32_sum", C.c_int32)]
 
 
 class View(C.Structure):

@@ -111,6 +111,17 @@ bool group_order_chosen(const gcoo_handle *h)
     return h->distinct_cols > 0 && 2 * h->nnz >= 3 * h->distinct_cols;
 }
 
+// The split summation's partial sums for B of n columns (grown, never
+// shrunk: allocated by the first multiply of a width, or by gcoo_prepare).
+gcoo_status ensure_split_work(gcoo_handle *h, int64_t n)
+{
+    if (h->pieces_bound <= 0)
+        return GCOO_SUCCESS;
+    if (!h->split_part.ensure(static_cast<size_t>(h->pieces_bound) * static_cast<size_t>(n)))
+        return fail(GCOO_ERROR_ALLOC, "device allocation of the long rows' partial sums failed");
+    return GCOO_SUCCESS;
+}
+
 gcoo_status spdm_fp32(gcoo_handle *h, const float *dB, int64_t n, float *dC, cudaStream_t st,
                       const gcoo_params *override_params)
 {
@@ -144,12 +155,21 @@ gcoo_status spdm_fp32(gcoo_handle *h, const float *dB, int64_t n, float *dC, cud
     // a skewed matrix (explicit launch-shape overrides aside): its long rows go
     // to their own kernel, the short rest to a kernel without staging
     if (!override_params && h->n_long > 0 && h->side && h->ev_fork && h->ev_join && long_rows_ok(n, dB)) {
+        const bool split = h->p.fp32_sum == GCOO_SUM_SPLIT && h->pieces_bound > 0;
+        if (split) {
+            gcoo_status ws = ensure_split_work(h, n);
+            if (ws != GCOO_SUCCESS)
+                return ws;
+        }
         // the two kernels write disjoint rows of C: the long rows run on the
         // side stream, forked from and joined back into the caller's stream
         GCOO_CUDA(cudaEventRecord(h->ev_fork, st));
         GCOO_CUDA(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
-        const cudaError_t el = launch_spdm_long(h->packed.ptr, h->row_ptr.ptr, h->long_rows.ptr, h->n_long, dB, n,
-                                                dC, h->side);
+        const cudaError_t el =
+            split ? launch_spdm_split(h->packed.ptr, h->row_ptr.ptr, h->long_rows.ptr, h->n_long, h->piece_first.ptr,
+                                      h->piece_row.ptr, h->piece_total.ptr, h->pieces_bound, dB, n,
+                                      h->split_part.ptr, dC, h->side)
+                  : launch_spdm_long(h->packed.ptr, h->row_ptr.ptr, h->long_rows.ptr, h->n_long, dB, n, dC, h->side);
         const cudaError_t es = el == cudaSuccess
                                    ? launch_spdm_short(h->packed.ptr, h->row_ptr.ptr, h->m, dB, n, dC, long_row_min(), st)
                                    : cudaSuccess;
@@ -157,7 +177,7 @@ gcoo_status spdm_fp32(gcoo_handle *h, const float *dB, int64_t n, float *dC, cud
         GCOO_CUDA(cudaEventRecord(h->ev_join, h->side));
         GCOO_CUDA(cudaStreamWaitEvent(st, h->ev_join, 0));
         if (el != cudaSuccess)
-            return cuda_fail(el, "spdm_long_kernel launch");
+            return cuda_fail(el, split ? "spdm_piece_kernel launch" : "spdm_long_kernel launch");
         if (es != cudaSuccess)
             return cuda_fail(es, "spdm_short_kernel launch");
         return GCOO_SUCCESS;
@@ -246,6 +266,8 @@ gcoo_status gcoo_create(gcoo_handle **out, const float *dA, int64_t m, int64_t k
         return fail(GCOO_ERROR_INVALID_VALUE, "fp32_order must be 0, 1 or 2");
     if (p.fp32_order == 2 && !group_order_ok(p.rows_per_group))
         return fail(GCOO_ERROR_UNSUPPORTED, "the group-order FP32 multiply needs rows_per_group 4");
+    if (p.fp32_sum != GCOO_SUM_CHAIN && p.fp32_sum != GCOO_SUM_SPLIT)
+        return fail(GCOO_ERROR_INVALID_VALUE, "fp32_sum must be GCOO_SUM_CHAIN (0) or GCOO_SUM_SPLIT (1)");
     gcoo_handle *h = new (std::nothrow) gcoo_handle();
     if (!h)
         return fail(GCOO_ERROR_ALLOC, "host allocation of the handle failed");
@@ -271,20 +293,34 @@ gcoo_status finish_build(gcoo_handle *h, cudaStream_t st)
     destroy_left_plan(h->left);
     h->left = nullptr;
     h->n_long = 0;
+    h->long_entries = 0;
+    h->pieces_bound = 0;
     if (row_lengths_skewed(h->m, h->nnz, h->max_row_nnz) && h->packed.count >= static_cast<size_t>(h->nnz) + 2) {
         const int64_t cap = h->nnz / long_row_min() + 1;
-        if (!h->long_rows.ensure(static_cast<size_t>(cap)) || !h->long_count.ensure(1))
+        if (!h->long_rows.ensure(static_cast<size_t>(cap)) || !h->long_count.ensure(2))
             return fail(GCOO_ERROR_ALLOC, "device allocation of the long-row list failed");
         unsigned long long *d_cnt = h->long_count.ptr;
-        GCOO_CUDA(cudaMemsetAsync(d_cnt, 0, sizeof(*d_cnt), st));
+        GCOO_CUDA(cudaMemsetAsync(d_cnt, 0, 2 * sizeof(*d_cnt), st));
         GCOO_CUDA(launch_collect_long(h->row_ptr.ptr, h->m, h->long_rows.ptr, cap, d_cnt, st));
+        const bool split = h->p.fp32_sum == GCOO_SUM_SPLIT;
+        if (split) {
+            // the piece plan, before the readback (its tables bounded without it)
+            const int64_t pcap = split_piece_bound(cap, h->nnz);
+            if (!h->piece_first.ensure(static_cast<size_t>(cap)) || !h->piece_row.ensure(static_cast<size_t>(pcap)) ||
+                !h->piece_total.ensure(1))
+                return fail(GCOO_ERROR_ALLOC, "device allocation of the long rows' piece plan failed");
+            GCOO_CUDA(launch_split_plan(h->row_ptr.ptr, h->long_rows.ptr, d_cnt, cap, h->piece_first.ptr,
+                                        h->piece_row.ptr, pcap, h->piece_total.ptr, st));
+        }
         if (!h->readback && cudaMallocHost(&h->readback, 4 * sizeof(int64_t)) != cudaSuccess) {
             h->readback = nullptr;
             return fail(GCOO_ERROR_ALLOC, "page-locked allocation of the readback words failed");
         }
-        GCOO_CUDA(cudaMemcpyAsync(h->readback, d_cnt, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        GCOO_CUDA(cudaMemcpyAsync(h->readback, d_cnt, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
         GCOO_CUDA(cudaStreamSynchronize(st));
         h->n_long = std::min<int64_t>(h->readback[0], cap);
+        h->long_entries = h->readback[1];
+        h->pieces_bound = split ? split_piece_bound(h->n_long, h->long_entries) : 0;
         if (h->n_long > 0) {
             // the long rows are the multiply's critical path: their CTAs go first
             // (each object made once; one that failed is retried by the next build)
@@ -511,8 +547,8 @@ gcoo_status gcoo_prepare(gcoo_handle *h, int64_t n, gcoo_precision prec, void *s
     gcoo_status s = check_n(n);
     if (s != GCOO_SUCCESS)
         return s;
-    if (prec == GCOO_PREC_FP32)
-        return GCOO_SUCCESS;
+    if (prec == GCOO_PREC_FP32) // the split summation's partial sums, if this handle sums in pieces
+        return h->p.fp32_sum == GCOO_SUM_SPLIT && h->n_long > 0 ? ensure_split_work(h, n) : GCOO_SUCCESS;
     if (prec < GCOO_PREC_FP32 || prec > GCOO_PREC_FP8_B)
         return fail(GCOO_ERROR_INVALID_VALUE, "unknown precision");
     return run_form(h, nullptr, n, nullptr, prec, static_cast<cudaStream_t>(stream), true);

@@ -45,8 +45,15 @@ struct gcoo_handle {
     gcoo::DevBuf<int32_t> over_list; // staged rebuild: the overflowed tiles
     int64_t *readback = nullptr;     // page-locked: the staged build's readback
     gcoo::DevBuf<int32_t> long_rows; // skewed matrices: rows multiplied by the long-row kernel
-    gcoo::DevBuf<unsigned long long> long_count;
+    gcoo::DevBuf<unsigned long long> long_count; // [0] long rows, [1] their entries
     int64_t n_long = 0;
+    int64_t long_entries = 0;
+    // fp32_sum = split: the piece plan of the long rows and the partial sums
+    gcoo::DevBuf<int32_t> piece_first;  // per long row: its first piece
+    gcoo::DevBuf<int32_t> piece_row;    // per piece: its long row (index into long_rows)
+    gcoo::DevBuf<int32_t> piece_total;  // pieces planned
+    gcoo::DevBuf<float> split_part;     // pieces x n partial sums (grown to the widest B)
+    int64_t pieces_bound = 0;
     // the long-row kernel runs beside the short-row one: a side stream joined by events
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;

@@ -183,6 +183,22 @@ bool long_rows_ok(int64_t n, const float *B);
 // list[0..min(*count, cap)) = the rows of at least long_row_min() entries (any order)
 cudaError_t launch_collect_long(const int32_t *row_ptr, int64_t m, int32_t *list, int64_t cap,
                                 unsigned long long *count, cudaStream_t st);
+// ---- long rows summed in pieces (spdm_split.cu, gcoo_params.fp32_sum = split) --------------
+// Pieces of a long-row list whose rows hold long_entries entries in total:
+// at most this many (also a bound for any list of n_long rows over nnz
+// entries with long_entries = nnz).
+int64_t split_piece_bound(int64_t n_long, int64_t long_entries);
+// The piece plan of the listed rows (count[0] of them, at most list_cap):
+// piece_first[row index], piece_row[piece] (at most cap pieces), *total.
+cudaError_t launch_split_plan(const int32_t *row_ptr, const int32_t *list, const unsigned long long *count,
+                              int64_t list_cap, int32_t *piece_first, int32_t *piece_row, int64_t cap,
+                              int32_t *total, cudaStream_t st);
+// C rows of the listed rows: partial sums per piece into part (pieces_bound
+// x n floats), then added in piece order. n % 4 == 0, B 16-byte aligned.
+cudaError_t launch_spdm_split(const Entry *packed, const int32_t *row_ptr, const int32_t *list, int64_t n_long,
+                              const int32_t *piece_first, const int32_t *piece_row, const int32_t *total,
+                              int64_t pieces_bound, const float *B, int64_t n, float *part, float *C,
+                              cudaStream_t st);
 // C rows of the listed rows, the same fmaf chains as launch_spdm_fp32
 cudaError_t launch_spdm_long(const Entry *packed, const int32_t *row_ptr, const int32_t *list, int64_t n_long,
                              const float *B, int64_t n, float *C, cudaStream_t st);

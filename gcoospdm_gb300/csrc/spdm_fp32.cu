@@ -291,13 +291,67 @@ spdm_fp32_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ r
     }
 }
 
-// The short rows of a skewed matrix (its long rows go to spdm_long.cu): one
-// warp per (row, 32*V-column tile), nothing staged and no CTA barrier -- a
-// row of a dozen entries is all latency, and the staging round trip and the
-// group's barrier would double it. Lane i loads entry i of each 32-entry
-// window; the B rows of eight entries at a time are loaded with their columns
-// shuffled from the owning lanes; each column's fmaf chain runs over the row's
-// entries in column order from 0.0f, as in every other FP32 kernel.
+// The short rows of a skewed matrix (its long rows go to spdm_long.cu or
+// spdm_split.cu): one warp per (row, 32*V-column tile), nothing staged and no
+// CTA barrier -- a row of a dozen entries is all latency, and a staging round
+// trip and a group barrier would double it. The row's two pointers come in
+// one load (lanes 0 and 1) and are shuffled to the warp. Lane i loads entry i
+// of each 32-entry window; the B rows of eight entries at a time are loaded
+// with their columns shuffled from the owning lanes; each column's fmaf chain
+// runs over the row's entries in column order from 0.0f, as in every other
+// FP32 kernel. Measured slower on the Zipf workload (0.148 ms for this
+// kernel with the long rows beside it): runs of 2-8 rows per warp with the
+// next row's entries requested early (0.158-0.171 ms), bundles of 2-8 rows
+// whose batches of eight entries run across row boundaries (0.159-0.211 ms),
+// and one warp on both 128-column tiles of a row (0.167 ms): at a dozen
+// entries per row, more independent warps in flight beat fewer round trips
+// per warp.
+template <int V>
+__device__ __forceinline__ void short_window(const Entry &my, int nw, bool all_cols, bool has_col,
+                                             const float *__restrict__ Bj, int64_t n, float (&acc)[V])
+{
+    int u0 = 0;
+    if (all_cols) { // warp-uniform: every lane takes part in the shuffles below
+        // whole batches of eight: no per-entry predicates
+        for (; u0 + 8 <= nw; u0 += 8) {
+            float a[8], b[8][V];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int col = __shfl_sync(0xffffffffu, my.col, u0 + u);
+                a[u] = __shfl_sync(0xffffffffu, my.val, u0 + u);
+                Vec<V>::load(Bj + static_cast<int64_t>(col) * n, b[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    acc[v] = fmaf(a[u], b[u][v], acc[v]);
+        }
+    }
+    // the tail batch (and lanes past n: shuffles only)
+    for (; u0 < nw; u0 += 8) {
+        float a[8], b[8][V];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int col = __shfl_sync(0xffffffffu, my.col, (u0 + u) & 31);
+            a[u] = __shfl_sync(0xffffffffu, my.val, (u0 + u) & 31);
+            if (u0 + u < nw && has_col) {
+                Vec<V>::load(Bj + static_cast<int64_t>(col) * n, b[u]);
+            } else {
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    b[u][v] = 0.0f;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (u0 + u < nw)
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    acc[v] = fmaf(a[u], b[u][v], acc[v]);
+    }
+}
+
 template <int V>
 __global__ void __launch_bounds__(64, 16)
 spdm_short_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ row_ptr, int64_t m,
@@ -309,11 +363,12 @@ spdm_short_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ 
     if (row >= m)
         return;
     const int t = static_cast<int>(gw - row * tiles);
-    const int64_t j = static_cast<int64_t>(t) * (32 * V) + static_cast<int64_t>(lane) * V;
-    const int32_t rs = row_ptr[row];
-    const int cnt = row_ptr[row + 1] - rs;
+    const int32_t rp = lane < 2 ? row_ptr[row + lane] : 0;
+    const int32_t rs = __shfl_sync(0xffffffffu, rp, 0);
+    const int cnt = __shfl_sync(0xffffffffu, rp, 1) - rs;
     if (long_min > 0 && cnt >= long_min)
         return; // the long-row kernel writes this row (warp-uniform)
+    const int64_t j = static_cast<int64_t>(t) * (32 * V) + static_cast<int64_t>(lane) * V;
     const bool has_col = j < n;
     const bool all_cols = __all_sync(0xffffffffu, has_col);
     const float *Bj = B + (has_col ? j : 0);
@@ -328,46 +383,7 @@ spdm_short_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ 
         my.val = 0.0f;
         if (lane < nw)
             my = packed[rs + w0 + lane];
-        int u0 = 0;
-        if (all_cols) { // warp-uniform: every lane takes part in the shuffles below
-            // whole batches of eight: no per-entry predicates
-            for (; u0 + 8 <= nw; u0 += 8) {
-                float a[8], b[8][V];
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const int col = __shfl_sync(0xffffffffu, my.col, u0 + u);
-                    a[u] = __shfl_sync(0xffffffffu, my.val, u0 + u);
-                    Vec<V>::load(Bj + static_cast<int64_t>(col) * n, b[u]);
-                }
-#pragma unroll
-                for (int u = 0; u < 8; ++u)
-#pragma unroll
-                    for (int v = 0; v < V; ++v)
-                        acc[v] = fmaf(a[u], b[u][v], acc[v]);
-            }
-        }
-        // the tail batch (and lanes past n: shuffles only)
-        for (; u0 < nw; u0 += 8) {
-            float a[8], b[8][V];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int col = __shfl_sync(0xffffffffu, my.col, (u0 + u) & 31);
-                a[u] = __shfl_sync(0xffffffffu, my.val, (u0 + u) & 31);
-                if (u0 + u < nw && has_col) {
-                    Vec<V>::load(Bj + static_cast<int64_t>(col) * n, b[u]);
-                } else {
-#pragma unroll
-                    for (int v = 0; v < V; ++v)
-                        b[u][v] = 0.0f;
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (u0 + u < nw)
-#pragma unroll
-                    for (int v = 0; v < V; ++v)
-                        acc[v] = fmaf(a[u], b[u][v], acc[v]);
-        }
+        short_window<V>(my, nw, all_cols, has_col, Bj, n, acc);
     }
     if (has_col)
         Vec<V>::store(C + row * n + j, acc);

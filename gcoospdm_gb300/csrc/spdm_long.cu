@@ -46,8 +46,10 @@ __global__ void collect_long_kernel(const int32_t *__restrict__ row_ptr, int64_t
 {
     for (int64_t r = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < m;
          r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        if (row_ptr[r + 1] - row_ptr[r] >= min_len) {
+        const int32_t len = row_ptr[r + 1] - row_ptr[r];
+        if (len >= min_len) {
             const unsigned long long i = atomicAdd(count, 1ull);
+            atomicAdd(count + 1, static_cast<unsigned long long>(len)); // the long rows' entries
             if (static_cast<int64_t>(i) < cap)
                 list[i] = static_cast<int32_t>(r);
         }

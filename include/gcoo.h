@@ -79,8 +79,22 @@ typedef struct gcoo_params {
                                (packed row order), 2 groups (GCOO order, one
                                B load per column shared by a group's rows;
                                groups of 4 rows). Both give the same bits. */
-    int32_t reserved;
+    int32_t fp32_sum;       /* gcoo_fp32_sum: summation of the FP32
+                               multiply's long rows (at least 256 entries,
+                               skewed matrices only)                      */
 } gcoo_params;
+
+/* FP32 summation order. CHAIN (the default): every output element is one
+ * sequential fmaf chain over its row's entries in column order from 0.0f,
+ * the reference kernel's order (src/gcoo_spdm_kernels.cu:129-139), so results
+ * are bit-identical to the reference's. SPLIT: in a skewed matrix (longest
+ * row >= 256 entries and above 8x the mean) the rows of >= 256 entries are
+ * summed as chains over pieces of 32 consecutive entries whose partial sums
+ * are then added in piece order: deterministic (the same bits on every run),
+ * not bit-identical to CHAIN, within FP32 rounding of the exact product
+ * (relative Frobenius error against FP64 of the order of 1e-7). Shorter rows
+ * and matrices that are not skewed keep the chain. */
+typedef enum gcoo_fp32_sum { GCOO_SUM_CHAIN = 0, GCOO_SUM_SPLIT = 1 } gcoo_fp32_sum;
 
 typedef struct gcoo_handle gcoo_handle;
 

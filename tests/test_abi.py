@@ -41,6 +41,20 @@ def test_params_default_is_reference_constant(native):
     p = native.Params()
     assert native.lib().gcoo_params_default(C.byref(p)) == 0
     assert p.rows_per_group == 4  # src/constants.h:4 COLUMN_PER_GROUP
+    assert p.fp32_sum == 0  # the sequential chain (the reference's order) by default
+
+
+@pytest.mark.parametrize("fp32_sum,err", [(0, 0), (1, 0), (2, 1), (-1, 1)])
+def test_create_checks_fp32_sum(native, fp32_sum, err):
+    L = native.lib()
+    h = C.c_void_p()
+    p = native.Params()
+    L.gcoo_params_default(C.byref(p))
+    p.fp32_sum = fp32_sum
+    st = L.gcoo_create(C.byref(h), C.c_void_p(0x1000), 8, 8, C.byref(p))  # the operand is not read here
+    assert st == err
+    if h.value:
+        assert L.gcoo_destroy(h) == 0
 
 
 @pytest.mark.parametrize("m,k,rpg,err", [(0, 5, 4, 1), (5, 0, 4, 1), (-1, 5, 4, 1), (1 << 31, 5, 4, 1),
