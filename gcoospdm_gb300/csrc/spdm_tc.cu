@@ -7,14 +7,15 @@
 //   * each active tile is stored densely (zeros where A has none) as BF16 in
 //     the K-major, 32-byte-swizzled shared-memory layout of tcgen05 (row r at
 //     r*32 bytes, 16-byte chunk c at (c ^ ((r >> 2) & 1)) * 16), so one 4 KB
-//     bulk copy lands it ready for the MMA; split-BF16 keeps a second (lo)
-//     tile;
+//     bulk copy lands it ready for the MMA; split-BF16 keeps two more tiles
+//     (lo = x - hi and lo2 = x - hi - lo, each rounded to BF16: hi + lo +
+//     lo2 is x exactly), stored side by side;
 //   * B is converted per call into tiles of N output columns x 16 k (the
 //     same layout, N rows of 32 bytes).
 // Kernel: one CTA per (panel, N-column tile); warp 0 streams the panel's
 // active tiles through an S-stage ring of shared-memory slots with
 // cp.async.bulk on mbarriers, warp 1 issues one tcgen05.mma kind::f16
-// (M=128, N, K=16; three for split-BF16) per tile into an FP32 accumulator in
+// (M=128, N, K=16; six for split-BF16) per tile into an FP32 accumulator in
 // tensor memory, tcgen05.commit frees each slot, and all four warps drain the
 // accumulator with tcgen05.ld into C. Every wait is bounded.
 #include <cuda_bf16.h>
@@ -36,10 +37,10 @@ struct TcPlan {
     DevBuf<int32_t> pf;       // exclusive prefix over (panel, cb) flags, size panels*kb + 1
     DevBuf<int32_t> tile_cb;  // cb of each tile (ascending within a panel)
     DevBuf<uint16_t> a_hi;    // tiles * 2048 bf16 (swizzled)
-    DevBuf<uint16_t> a_lo;    // split only
+    DevBuf<uint16_t> a_lo;    // split only: tiles * 2 * 2048 bf16 (lo, then lo2, per tile)
     DevBuf<int64_t> scratch;
     // B workspace (per call)
-    DevBuf<uint16_t> b_hi, b_lo;
+    DevBuf<uint16_t> b_hi, b_lo; // b_lo (split only): lo then lo2 per B tile
     int64_t b_n = 0;
     // FP8-B: per-column power-of-two scales (and their absmax scratch)
     DevBuf<float> b_scale;
@@ -149,8 +150,12 @@ __global__ void tile_fill_kernel(const Entry *__restrict__ packed, const int32_t
             const uint32_t off = sw32_offset(lr, static_cast<uint32_t>(t.col % kTileK)) / 2;
             const __nv_bfloat16 h = __float2bfloat16_rn(t.val);
             hi[tile * (kTileBytes / 2) + off] = h;
-            if (lo)
-                lo[tile * (kTileBytes / 2) + off] = __float2bfloat16_rn(t.val - __bfloat162float(h));
+            if (lo) {
+                const float r1 = t.val - __bfloat162float(h); // exact
+                const __nv_bfloat16 l1 = __float2bfloat16_rn(r1);
+                lo[tile * kTileBytes + off] = l1;
+                lo[tile * kTileBytes + kTileBytes / 2 + off] = __float2bfloat16_rn(r1 - __bfloat162float(l1));
+            }
         }
     }
 }
@@ -159,40 +164,73 @@ __global__ void tile_fill_kernel(const Entry *__restrict__ packed, const int32_t
 // With fp8_scale (FP8-B): each value is first quantized to E4M3 in units of
 // its column's power-of-two scale, then stored as the exact BF16 value of
 // E4M3 x scale, so the BF16 MMA multiplies the FP8-B operand exactly.
-__global__ void b_tiles_kernel(const float *__restrict__ B, int64_t k, int64_t n, int N, int64_t kb,
-                               __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo,
-                               const float *__restrict__ fp8_scale)
+// Each pair of lanes builds one 32-byte tile row (output column j): lane
+// half h converts B[cb*16 + 8h .. + 8][j] and stores them as one 16-byte
+// chunk, so a warp writes 16 whole rows (no partial-sector stores) while
+// its loads read 16 consecutive columns of two B rows at a time.
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo_half, __nv_bfloat16 hi_half)
+{
+    return static_cast<uint32_t>(__bfloat16_as_ushort(lo_half)) |
+           (static_cast<uint32_t>(__bfloat16_as_ushort(hi_half)) << 16);
+}
+
+__global__ void __launch_bounds__(256)
+b_tiles_kernel(const float *__restrict__ B, int64_t k, int64_t n, int N, int64_t kb, __nv_bfloat16 *__restrict__ hi,
+               __nv_bfloat16 *__restrict__ lo, const float *__restrict__ fp8_scale)
 {
     const int64_t cb = blockIdx.x;
     const int64_t jt = blockIdx.y;
     const int64_t tile = jt * kb + cb;
     const size_t tile_elems = static_cast<size_t>(N) * kTileK;
-    for (int idx = threadIdx.x; idx < N * kTileK; idx += blockDim.x) {
-        const int jj = idx % N;          // consecutive threads: consecutive columns of B (coalesced reads)
-        const int kk = idx / N;
-        const int64_t c = cb * kTileK + kk;
+    const int half = threadIdx.x & 1;
+    for (int jj = threadIdx.x >> 1; jj < N; jj += blockDim.x >> 1) {
         const int64_t j = jt * N + jj;
-        float v = (c < k && j < n) ? __ldg(B + c * n + j) : 0.0f;
-        if (fp8_scale && j < n) {
-            const float sc = fp8_scale[j];
-            const __nv_fp8_storage_t q = __nv_cvt_float_to_fp8(v / sc, __NV_SATFINITE, __NV_E4M3);
-            v = __half2float(__half(__nv_cvt_fp8_to_halfraw(q, __NV_E4M3))) * sc;
+        float sc = 1.0f;
+        if (fp8_scale && j < n)
+            sc = fp8_scale[j];
+        uint32_t wh[4], wl[4], wl2[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            __nv_bfloat16 h2[2], l2[2], m2[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int64_t c = cb * kTileK + half * 8 + q * 2 + e;
+                float v = (c < k && j < n) ? __ldg(B + c * n + j) : 0.0f;
+                if (fp8_scale && j < n) {
+                    const __nv_fp8_storage_t f8 = __nv_cvt_float_to_fp8(v / sc, __NV_SATFINITE, __NV_E4M3);
+                    v = __half2float(__half(__nv_cvt_fp8_to_halfraw(f8, __NV_E4M3))) * sc;
+                }
+                h2[e] = __float2bfloat16_rn(v);
+                const float r1 = v - __bfloat162float(h2[e]); // exact
+                l2[e] = __float2bfloat16_rn(r1);
+                m2[e] = __float2bfloat16_rn(r1 - __bfloat162float(l2[e]));
+            }
+            wh[q] = pack_bf16(h2[0], h2[1]);
+            wl[q] = pack_bf16(l2[0], l2[1]);
+            wl2[q] = pack_bf16(m2[0], m2[1]);
         }
-        const uint32_t off = sw32_offset(static_cast<uint32_t>(jj), static_cast<uint32_t>(kk)) / 2;
-        const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        hi[tile * tile_elems + off] = h;
-        if (lo)
-            lo[tile * tile_elems + off] = __float2bfloat16_rn(v - __bfloat162float(h));
+        const uint32_t off = sw32_offset(static_cast<uint32_t>(jj), static_cast<uint32_t>(half * 8)) / 2;
+        *reinterpret_cast<uint4 *>(hi + tile * tile_elems + off) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+        if (lo) {
+            *reinterpret_cast<uint4 *>(lo + 2 * tile * tile_elems + off) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
+            *reinterpret_cast<uint4 *>(lo + (2 * tile + 1) * tile_elems + off) =
+                make_uint4(wl2[0], wl2[1], wl2[2], wl2[3]);
+        }
     }
 }
 
 // ---- the MMA kernel ---------------------------------------------------------------------
 template <int N, int S, bool SPLIT>
 struct TcCfg {
-    static constexpr int kABytes = kTileBytes * (SPLIT ? 2 : 1);
-    static constexpr int kBBytes = N * 32 * (SPLIT ? 2 : 1);
+    static constexpr int kABytes = kTileBytes * (SPLIT ? 3 : 1); // hi (, lo, lo2)
+    static constexpr int kBBytes = N * 32 * (SPLIT ? 3 : 1);
     static constexpr int kStage = kABytes + kBBytes;
+    static constexpr int kBanks = SPLIT ? 2 : 1;       // accumulators of N columns each
+    static constexpr int kTmemCols = N * kBanks;       // a power of two in [32, 512]
     static constexpr int kSmem = 1024 /* barriers, tmem slot */ + S * kStage + 1024 /* alignment slack */;
+    static_assert(kTmemCols >= 32 && kTmemCols <= 512 && (kTmemCols & (kTmemCols - 1)) == 0,
+                  "tensor memory is allocated in powers of two of at most 512 columns");
+    static_assert(kSmem <= 227 * 1024, "the ring must fit one CTA's shared memory");
 };
 
 template <int N, int S, bool SPLIT>
@@ -231,7 +269,7 @@ spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_
     }
     if (warp == 2) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(N * (SPLIT ? 2 : 1))
+                     "r"(Cfg::kTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -239,10 +277,12 @@ spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    // split-BF16 alternates two accumulator banks by tile parity (shorter
-    // FP32 accumulation chains in the tensor pipe); the epilogue adds them
-    constexpr int BANKS = SPLIT ? 2 : 1;
-    const int banks_used = ntiles >= BANKS ? BANKS : 1;
+    // split-BF16 keeps the leading products (ah * bh) in bank 0 and the five
+    // correction products in bank 1, so each correction is rounded at its
+    // own (2^-8 smaller) magnitude, not at the running total's; the epilogue
+    // adds bank 1 to bank 0
+    constexpr int BANKS = Cfg::kBanks;
+    const int banks_used = BANKS;
 
     if (ntiles > 0) {
         if (warp == 0 && lane == 0) {
@@ -262,9 +302,9 @@ spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_
                 mbar_arrive_expect_tx(&full[s], Cfg::kStage);
                 bulk_g2s(st, a_hi + tile * (kTileBytes / 2), kTileBytes, &full[s]);
                 bulk_g2s(st + Cfg::kABytes, b_hi + btile * (N * 16), N * 32, &full[s]);
-                if (SPLIT) {
-                    bulk_g2s(st + kTileBytes, a_lo + tile * (kTileBytes / 2), kTileBytes, &full[s]);
-                    bulk_g2s(st + Cfg::kABytes + N * 32, b_lo + btile * (N * 16), N * 32, &full[s]);
+                if (SPLIT) { // lo and lo2 of A, then of B: one contiguous copy each
+                    bulk_g2s(st + kTileBytes, a_lo + tile * kTileBytes, 2 * kTileBytes, &full[s]);
+                    bulk_g2s(st + Cfg::kABytes + N * 32, b_lo + btile * (N * 32), 2 * N * 32, &full[s]);
                 }
             }
         } else if (warp == 1 && lane == 0) {
@@ -282,15 +322,21 @@ spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_
                 const uint32_t st = smem_u32(stages + static_cast<size_t>(s) * Cfg::kStage);
                 const uint64_t ah = smem_desc_sw32(st);
                 const uint64_t bh = smem_desc_sw32(st + Cfg::kABytes);
-                const uint32_t d = tmem + static_cast<uint32_t>((i % BANKS) * N);
-                tc_mma(d, ah, bh, idesc, i >= BANKS ? 1u : 0u);
+                tc_mma(tmem, ah, bh, idesc, i > 0 ? 1u : 0u);
                 if (SPLIT) {
-                    // (ah + al)(bh + bl): all four products
+                    // (ah + al + al2)(bh + bl + bl2): every product above 2^-24
+                    // of the leading one (al * bl2, al2 * bl, al2 * bl2 dropped),
+                    // into the correction bank
+                    const uint32_t dx = tmem + static_cast<uint32_t>(N);
                     const uint64_t al = smem_desc_sw32(st + kTileBytes);
+                    const uint64_t al2 = smem_desc_sw32(st + 2 * kTileBytes);
                     const uint64_t bl = smem_desc_sw32(st + Cfg::kABytes + N * 32);
-                    tc_mma(d, ah, bl, idesc, 1u);
-                    tc_mma(d, al, bh, idesc, 1u);
-                    tc_mma(d, al, bl, idesc, 1u);
+                    const uint64_t bl2 = smem_desc_sw32(st + Cfg::kABytes + 2 * N * 32);
+                    tc_mma(dx, ah, bl, idesc, i > 0 ? 1u : 0u);
+                    tc_mma(dx, al, bh, idesc, 1u);
+                    tc_mma(dx, al, bl, idesc, 1u);
+                    tc_mma(dx, ah, bl2, idesc, 1u);
+                    tc_mma(dx, al2, bh, idesc, 1u);
                 }
                 tc_commit(&empty[s]); // slot reusable once these MMAs have read it
             }
@@ -308,9 +354,9 @@ spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_
             for (int c = 0; c < N; c += 32) {
                 float v[32];
                 tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c), v);
-                if (BANKS == 2 && banks_used == 2) {
+                for (int bank = 1; bank < banks_used; ++bank) {
                     float w[32];
-                    tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(N + c), w);
+                    tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(bank * N + c), w);
 #pragma unroll
                     for (int q = 0; q < 32; ++q)
                         v[q] += w[q];
@@ -347,14 +393,15 @@ spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_
     __syncthreads();
     if (warp == 2) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(N * (SPLIT ? 2 : 1))
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cfg::kTmemCols)
                      : "memory");
     }
 }
 
 // Output columns per CTA. A CTA's ring is sized (~98 KB) so that two CTAs
 // share an SM; split-BF16 keeps two accumulator banks, so it uses 128-column
-// tiles to stay within half of the 512 tensor-memory columns.
+// tiles to stay within half of the 512 tensor-memory columns. (Four banks in
+// all 512 columns, one CTA per SM with a 12-stage ring, measured 1.8x slower.)
 int tile_n_for(int64_t n, bool split) { return (!split && n >= 256) ? 256 : 128; }
 
 template <int N, int S, bool SPLIT>
@@ -404,14 +451,14 @@ gcoo_status tc_build_plan(gcoo_handle *h, bool split, cudaStream_t st)
     p.tiles = total;
     const size_t tile_elems = static_cast<size_t>(kTileBytes / 2);
     if (!p.tile_cb.ensure(total + 1) || !p.a_hi.ensure(total * tile_elems + 1) ||
-        (split && !p.a_lo.ensure(total * tile_elems + 1)))
+        (split && !p.a_lo.ensure(2 * total * tile_elems + 1)))
         return fail(GCOO_ERROR_ALLOC, "device allocation of the dense tiles failed");
     if (total > 0) {
         tile_list_kernel<<<static_cast<unsigned>(std::min<int64_t>((L + 255) / 256, 4096)), 256, 0, st>>>(p.pf.ptr, L,
                                                                                                           p.kb, p.tile_cb.ptr);
         GCOO_CUDA(cudaMemsetAsync(p.a_hi.ptr, 0, total * kTileBytes, st));
         if (split)
-            GCOO_CUDA(cudaMemsetAsync(p.a_lo.ptr, 0, total * kTileBytes, st));
+            GCOO_CUDA(cudaMemsetAsync(p.a_lo.ptr, 0, 2 * total * kTileBytes, st));
         tile_fill_kernel<<<blocks, 256, 0, st>>>(h->packed.ptr, h->row_ptr.ptr, h->m, p.kb, p.pf.ptr,
                                                  reinterpret_cast<__nv_bfloat16 *>(p.a_hi.ptr),
                                                  split ? reinterpret_cast<__nv_bfloat16 *>(p.a_lo.ptr) : nullptr);
@@ -435,7 +482,7 @@ gcoo_status tc_prepare_b(gcoo_handle *h, int64_t n, bool fp8)
     const int N = tile_n_for(n, p.split);
     const int64_t nt = (n + N - 1) / N;
     const size_t elems = static_cast<size_t>(nt) * p.kb * N * kTileK;
-    if (!p.b_hi.ensure(elems) || (p.split && !p.b_lo.ensure(elems)) ||
+    if (!p.b_hi.ensure(elems) || (p.split && !p.b_lo.ensure(2 * elems)) ||
         (fp8 && (!p.b_scale.ensure(static_cast<size_t>(n)) || !p.b_amax.ensure(static_cast<size_t>(n)))))
         return fail(GCOO_ERROR_ALLOC, "device allocation of the B tiles failed");
     p.b_n = n;
@@ -460,7 +507,7 @@ gcoo_status tc_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, bool 
     else if (N == 128 && !p.split)
         e = launch_tc<128, 12, false>(p, h->m, n, dC, h->status.ptr, st);
     else
-        e = launch_tc<128, 6, true>(p, h->m, n, dC, h->status.ptr, st);
+        e = launch_tc<128, 4, true>(p, h->m, n, dC, h->status.ptr, st);
     if (e != cudaSuccess)
         return cuda_fail(e, "spdm_tc_kernel launch");
     return GCOO_SUCCESS;
