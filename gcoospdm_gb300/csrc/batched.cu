@@ -12,8 +12,11 @@
 // results are bit-identical to gcoo_spdm per problem and BF16 results to
 // gcoo_spdm_ex(BF16) on the FMA engine.
 //
-// rows_per_item is chosen per shape bucket (n and density class) by timing
-// the candidates on that bucket's items (the autotune table, persisted with
+// The item shape -- rows_per_item and the per-lane vector width (FP32 up to
+// 4 floats, BF16 up to 8 values: one 16-byte load per entry), which sets the
+// lanes per row (n / width, 4 to 32: several narrow rows share a warp) -- is
+// chosen per shape bucket (n and density class) by timing the candidates on
+// that bucket's items (the autotune table, persisted with
 // gcoo_autotune_save); a loaded table skips the timing.
 #include <cuda_bf16.h>
 #include <math.h>
@@ -37,7 +40,9 @@ struct BatchProb {
 };
 
 struct BatchItem {
-    int32_t prob, row0, row1, vec;
+    int32_t prob, row0, row1;
+    int16_t vec; // values of B per lane and load
+    int16_t lpr; // lanes per row: a warp runs 32 / lpr rows side by side
 };
 
 struct ConvSeg {
@@ -82,10 +87,12 @@ namespace {
 
 constexpr int kBatchThreads = 256;
 
+// B loads of V values per lane: FP32 (V floats) or the BF16 copy (V bf16
+// values, half the bytes), widened to FP32.
 template <int V, bool BF16>
-struct BLoad;
+struct RowLoad;
 template <int V>
-struct BLoad<V, false> {
+struct RowLoad<V, false> {
     static __device__ __forceinline__ void load(const BatchProb &p, int64_t off, float (&b)[V])
     {
         if constexpr (V == 4) {
@@ -100,29 +107,61 @@ struct BLoad<V, false> {
     }
 };
 template <int V>
-struct BLoad<V, true> {
+struct RowLoad<V, true> {
     static __device__ __forceinline__ void load(const BatchProb &p, int64_t off, float (&b)[V])
     {
-        if constexpr (V == 4) {
-            const uint2 t = __ldg(reinterpret_cast<const uint2 *>(p.Bbf + off));
+        const uint16_t *q = p.Bbf + off;
+        if constexpr (V == 8) {
+            const uint4 t = __ldg(reinterpret_cast<const uint4 *>(q));
+            b[0] = __uint_as_float(t.x << 16); b[1] = __uint_as_float(t.x & 0xffff0000u);
+            b[2] = __uint_as_float(t.y << 16); b[3] = __uint_as_float(t.y & 0xffff0000u);
+            b[4] = __uint_as_float(t.z << 16); b[5] = __uint_as_float(t.z & 0xffff0000u);
+            b[6] = __uint_as_float(t.w << 16); b[7] = __uint_as_float(t.w & 0xffff0000u);
+        } else if constexpr (V == 4) {
+            const uint2 t = __ldg(reinterpret_cast<const uint2 *>(q));
             b[0] = __uint_as_float(t.x << 16); b[1] = __uint_as_float(t.x & 0xffff0000u);
             b[2] = __uint_as_float(t.y << 16); b[3] = __uint_as_float(t.y & 0xffff0000u);
         } else if constexpr (V == 2) {
-            const uint32_t t = __ldg(reinterpret_cast<const unsigned int *>(p.Bbf + off));
+            const uint32_t t = __ldg(reinterpret_cast<const unsigned int *>(q));
             b[0] = __uint_as_float(t << 16); b[1] = __uint_as_float(t & 0xffff0000u);
         } else {
-            b[0] = __uint_as_float(static_cast<uint32_t>(__ldg(reinterpret_cast<const unsigned short *>(p.Bbf + off))) << 16);
+            b[0] = __uint_as_float(static_cast<uint32_t>(__ldg(reinterpret_cast<const unsigned short *>(q))) << 16);
         }
     }
 };
 
-template <int V, bool BF16>
+template <int V>
+__device__ __forceinline__ void store_row(float *out, const float (&acc)[V])
+{
+    if constexpr (V == 8) {
+        reinterpret_cast<float4 *>(out)[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+        reinterpret_cast<float4 *>(out)[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+    } else if constexpr (V == 4) {
+        *reinterpret_cast<float4 *>(out) = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    } else if constexpr (V == 2) {
+        *reinterpret_cast<float2 *>(out) = make_float2(acc[0], acc[1]);
+    } else {
+        out[0] = acc[0];
+    }
+}
+
+// The rows of an item, LPR lanes per row (32 / LPR rows per warp side by
+// side), V values of B per lane and load; each lane runs its columns' fmaf
+// chains over the row's entries in order, batches of four entries' loads in
+// flight; a = the entry (BF16: rounded to bf16). The same chains for every
+// (V, LPR), so results do not depend on the shape.
+template <int V, int LPR, bool BF16>
 __device__ __forceinline__ void item_rows(const BatchProb &p, int row0, int row1, int warp, int lane)
 {
     constexpr int W = kBatchThreads / 32;
-    for (int row = row0 + warp; row < row1; row += W) {
+    constexpr int RPW = 32 / LPR;
+    const int sub = lane / LPR, sl = lane % LPR;
+    for (int rb = row0 + RPW * warp; rb < row1; rb += RPW * W) {
+        const int row = rb + sub;
+        if (row >= row1)
+            continue; // no row for this lane group (nothing warp-wide below)
         const int64_t e0 = p.row_ptr[row], e1 = p.row_ptr[row + 1];
-        for (int64_t j = static_cast<int64_t>(lane) * V; j < p.n; j += 32 * V) {
+        for (int64_t j = static_cast<int64_t>(sl) * V; j < p.n; j += LPR * V) {
             float acc[V];
 #pragma unroll
             for (int v = 0; v < V; ++v)
@@ -137,7 +176,7 @@ __device__ __forceinline__ void item_rows(const BatchProb &p, int row0, int row1
                     t[u] = p.packed[e + u];
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
-                    BLoad<V, BF16>::load(p, static_cast<int64_t>(t[u].col) * p.n + j, b[u]);
+                    RowLoad<V, BF16>::load(p, static_cast<int64_t>(t[u].col) * p.n + j, b[u]);
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const float a = BF16 ? __bfloat162float(__float2bfloat16_rn(t[u].val)) : t[u].val;
@@ -150,18 +189,32 @@ __device__ __forceinline__ void item_rows(const BatchProb &p, int row0, int row1
             for (; e < e1; ++e) {
                 const Entry t = p.packed[e];
                 float b[V];
-                BLoad<V, BF16>::load(p, static_cast<int64_t>(t.col) * p.n + j, b);
+                RowLoad<V, BF16>::load(p, static_cast<int64_t>(t.col) * p.n + j, b);
                 const float a = BF16 ? __bfloat162float(__float2bfloat16_rn(t.val)) : t.val;
 #pragma unroll
                 for (int v = 0; v < V; ++v)
                     acc[v] = fmaf(a, b[v], acc[v]);
             }
-            float *out = p.C + static_cast<int64_t>(row) * p.n + j;
-#pragma unroll
-            for (int v = 0; v < V; ++v)
-                out[v] = acc[v];
+            store_row<V>(p.C + static_cast<int64_t>(row) * p.n + j, acc);
         }
     }
+}
+
+// The (V, LPR) shapes an item may take.
+template <bool BF16>
+__device__ __forceinline__ void run_item(const BatchProb &p, const BatchItem &w, int warp, int lane)
+{
+#define GCOO_ITEM(V, L)                                                                                 \
+    if (w.vec == V && w.lpr == L) {                                                                     \
+        item_rows<V, L, BF16>(p, w.row0, w.row1, warp, lane);                                           \
+        return;                                                                                         \
+    }
+    if constexpr (BF16) {
+        GCOO_ITEM(8, 4) GCOO_ITEM(8, 8) GCOO_ITEM(8, 16)
+    }
+    GCOO_ITEM(4, 8) GCOO_ITEM(4, 16) GCOO_ITEM(4, 32) GCOO_ITEM(2, 16) GCOO_ITEM(2, 32)
+#undef GCOO_ITEM
+    item_rows<1, 32, BF16>(p, w.row0, w.row1, warp, lane); // any n, any alignment
 }
 
 // Persistent: CTAs pull work items from the queue with an atomic counter.
@@ -182,12 +235,7 @@ batch_kernel(const BatchProb *__restrict__ probs, const BatchItem *__restrict__ 
             break;
         const BatchItem w = items[it];
         const BatchProb p = probs[w.prob];
-        if (w.vec == 4)
-            item_rows<4, BF16>(p, w.row0, w.row1, warp, lane);
-        else if (w.vec == 2)
-            item_rows<2, BF16>(p, w.row0, w.row1, warp, lane);
-        else
-            item_rows<1, BF16>(p, w.row0, w.row1, warp, lane);
+        run_item<BF16>(p, w, warp, lane);
     }
 }
 
@@ -204,14 +252,40 @@ __global__ void batch_bf16_kernel(const ConvSeg *__restrict__ segs)
     }
 }
 
+// Widest load per lane (values of B) for a problem: 16-byte loads where n and
+// the alignment of B and C allow (the BF16 copy of B is 32-byte aligned per
+// problem, so there n and C decide).
+int pick_vec_bf16(int64_t n, const float *C)
+{
+    const uintptr_t c = reinterpret_cast<uintptr_t>(C);
+    if (n % 8 == 0 && (c & 15) == 0)
+        return 8;
+    if (n % 4 == 0 && (c & 15) == 0)
+        return 4;
+    if (n % 2 == 0 && (c & 7) == 0)
+        return 2;
+    return 1;
+}
+
 int pick_vec(int64_t n, const float *B, const float *C)
 {
     const uintptr_t a = reinterpret_cast<uintptr_t>(B) | reinterpret_cast<uintptr_t>(C);
-    if (n >= 128 && n % 4 == 0 && (a & 15) == 0)
+    if (n % 4 == 0 && (a & 15) == 0)
         return 4;
-    if (n >= 64 && n % 2 == 0 && (a & 7) == 0)
+    if (n % 2 == 0 && (a & 7) == 0)
         return 2;
     return 1;
+}
+
+// Lanes per row for V values per lane: enough to cover n in one pass, a power
+// of two between the narrowest shape the kernel has for V and 32.
+int lanes_per_row(int64_t n, int vec)
+{
+    const int lo = vec == 8 ? 4 : vec == 4 ? 8 : vec == 2 ? 16 : 32;
+    int l = 32;
+    while (l > lo && static_cast<int64_t>(l / 2) * vec >= n)
+        l /= 2;
+    return l;
 }
 
 std::string batch_bucket(const gcoo_problem &p)
@@ -225,17 +299,27 @@ std::string batch_bucket(const gcoo_problem &p)
     return "batch_n" + std::to_string(ln) + "_d" + std::to_string(d);
 }
 
-void make_items(const gcoo_batch &b, const std::vector<int> &probs, const std::map<std::string, int> &rpi,
+// A bucket's tuned shape: rows per work item and the widest per-lane vector
+// (a cap on each problem's widest valid width).
+struct ItemShape {
+    int rows = 16;
+    int vec_cap = 8;
+};
+
+void make_items(const gcoo_batch &b, const std::vector<int> &probs, const std::map<std::string, ItemShape> &shape,
                 std::vector<BatchItem> &items)
 {
     std::vector<std::pair<int64_t, BatchItem>> tmp;
     for (int i : probs) {
-        const int r = rpi.at(b.bucket[i]);
+        const ItemShape &sh = shape.at(b.bucket[i]);
+        const int r = sh.rows;
+        const int vec = std::min(b.vec[i], std::max(1, sh.vec_cap));
+        const int lpr = lanes_per_row(b.probs[i].n, vec);
         const std::vector<int32_t> &rp = b.row_ptr_h[i];
         const int m = static_cast<int>(rp.size()) - 1;
         for (int r0 = 0; r0 < m; r0 += r) {
             const int r1 = std::min(m, r0 + r);
-            BatchItem it{i, r0, r1, b.vec[i]};
+            BatchItem it{i, r0, r1, static_cast<int16_t>(vec), static_cast<int16_t>(lpr)};
             tmp.push_back({static_cast<int64_t>(rp[r1] - rp[r0]) * b.probs[i].n + (r1 - r0), it});
         }
     }
@@ -309,7 +393,7 @@ gcoo_status gcoo_batch_create(gcoo_batch **out, const gcoo_problem *problems, in
     int64_t bf_total = 0;
     for (int32_t i = 0; i < count; ++i) {
         const gcoo_problem &p = problems[i];
-        b->vec[i] = pick_vec(p.n, p.dB, p.dC);
+        b->vec[i] = prec == GCOO_PREC_BF16 ? pick_vec_bf16(p.n, p.dC) : pick_vec(p.n, p.dB, p.dC);
         b->bucket[i] = batch_bucket(p);
         if (prec == GCOO_PREC_BF16) {
             bf_off[i] = bf_total;
@@ -355,7 +439,7 @@ gcoo_status gcoo_batch_create(gcoo_batch **out, const gcoo_problem *problems, in
     std::map<std::string, std::vector<int>> by_bucket;
     for (int32_t i = 0; i < count; ++i)
         by_bucket[b->bucket[i]].push_back(i);
-    std::map<std::string, int> rpi;
+    std::map<std::string, ItemShape> shapes;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
         if (e0)
@@ -366,13 +450,20 @@ gcoo_status gcoo_batch_create(gcoo_batch **out, const gcoo_problem *problems, in
         const std::string key = kv.first + (prec == GCOO_PREC_BF16 ? "_bf16" : "_fp32");
         TuneEntry te;
         if (tune_lookup(key, &te) && te.rows_per_item > 0) {
-            rpi[kv.first] = te.rows_per_item;
+            shapes[kv.first] = ItemShape{te.rows_per_item, te.vec > 0 ? te.vec : 8};
             continue;
         }
+        int vmax = 1;
+        for (int i : kv.second)
+            vmax = std::max(vmax, b->vec[i]);
         float best = 1e30f;
-        int best_r = 16;
-        for (int r : {4, 8, 16, 32, 64}) {
-            std::map<std::string, int> one = {{kv.first, r}};
+        ItemShape best_sh{16, vmax};
+        for (int vc : {vmax, vmax / 2})
+            for (int r : {4, 8, 16, 32, 64}) {
+            if (vc < 1 || (vc == vmax / 2 && vmax == 1))
+                continue;
+            const ItemShape sh{r, vc};
+            std::map<std::string, ItemShape> one = {{kv.first, sh}};
             std::vector<BatchItem> items;
             make_items(*b, kv.second, one, items);
             const gcoo_status us = upload_items(*b, items, st);
@@ -394,12 +485,13 @@ gcoo_status gcoo_batch_create(gcoo_batch **out, const gcoo_problem *problems, in
             }
             if (ms_min < best) {
                 best = ms_min;
-                best_r = r;
+                best_sh = sh;
             }
         }
-        rpi[kv.first] = best_r;
+        shapes[kv.first] = best_sh;
         te = TuneEntry();
-        te.rows_per_item = best_r;
+        te.rows_per_item = best_sh.rows;
+        te.vec = best_sh.vec_cap;
         te.us = best * 1e3;
         tune_store(key, te);
     }
@@ -412,7 +504,7 @@ gcoo_status gcoo_batch_create(gcoo_batch **out, const gcoo_problem *problems, in
     for (int32_t i = 0; i < count; ++i)
         all[i] = i;
     std::vector<BatchItem> items;
-    make_items(*b, all, rpi, items);
+    make_items(*b, all, shapes, items);
     gcoo_status s = upload_items(*b, items, st);
     if (s != GCOO_SUCCESS)
         return bail(s);
