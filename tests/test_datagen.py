@@ -87,3 +87,10 @@ def test_batched_shapes_ranges():
     assert set(n.tolist()) == {32, 64, 128}
     assert sp.min() >= 0.9 and sp.max() < 0.999
     assert dg.batched_shapes(777, 512) == s          # deterministic
+
+
+def test_bernoulli_nnz_counts_the_mask():
+    """The mask count the bench's reference arm reports without building A."""
+    for seed, m, k, p in ((3, 37, 129, 0.05), (8192, 300, 8192, 0.01), (9, 1, 5000, 0.5)):
+        A = dg.bernoulli_dense(seed, m, k, p)
+        assert dg.bernoulli_nnz(seed, m, k, p) == int(np.count_nonzero(A))
