@@ -6,8 +6,8 @@
 // into a device queue, and captures [queue reset, (B -> BF16), persistent
 // kernel] into a CUDA graph on a private stream. gcoo_batch_run replays that
 // graph on the caller's stream: one kernel launch (two for BF16) whatever the
-// number of problems. CTAs of the persistent kernel pull items with an atomic
-// counter (no waits on other CTAs); each warp computes whole rows of an item
+// number of problems. Warps of the persistent kernel pull items with an
+// atomic counter (no waits on other warps); each warp computes whole rows of an item
 // with the same sequential fmaf chain as the single-problem kernels, so FP32
 // results are bit-identical to gcoo_spdm per problem and BF16 results to
 // gcoo_spdm_ex(BF16) on the FMA engine.
@@ -153,7 +153,7 @@ __device__ __forceinline__ void store_row(float *out, const float (&acc)[V])
 template <int V, int LPR, bool BF16>
 __device__ __forceinline__ void item_rows(const BatchProb &p, int row0, int row1, int warp, int lane)
 {
-    constexpr int W = kBatchThreads / 32;
+    constexpr int W = 1; // one warp per item
     constexpr int RPW = 32 / LPR;
     const int sub = lane / LPR, sl = lane % LPR;
     for (int rb = row0 + RPW * warp; rb < row1; rb += RPW * W) {
@@ -217,25 +217,25 @@ __device__ __forceinline__ void run_item(const BatchProb &p, const BatchItem &w,
     item_rows<1, 32, BF16>(p, w.row0, w.row1, warp, lane); // any n, any alignment
 }
 
-// Persistent: CTAs pull work items from the queue with an atomic counter.
+// Persistent: every warp pulls work items from the queue with an atomic
+// counter (no CTA barrier between items: a warp that finishes early takes
+// the next item; the queue is sorted by work, longest first).
 template <bool BF16>
 __global__ void __launch_bounds__(kBatchThreads)
 batch_kernel(const BatchProb *__restrict__ probs, const BatchItem *__restrict__ items, int nitems,
              unsigned *__restrict__ counter)
 {
-    __shared__ int s_item;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31;
     for (;;) {
-        __syncthreads(); // everyone has read the previous item index
-        if (threadIdx.x == 0)
-            s_item = static_cast<int>(atomicAdd(counter, 1u));
-        __syncthreads();
-        const int it = s_item;
-        if (it >= nitems)
-            break;
+        unsigned it = 0;
+        if (lane == 0)
+            it = atomicAdd(counter, 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= static_cast<unsigned>(nitems))
+            break; // warp-uniform
         const BatchItem w = items[it];
         const BatchProb p = probs[w.prob];
-        run_item<BF16>(p, w, warp, lane);
+        run_item<BF16>(p, w, 0, lane);
     }
 }
 
