@@ -87,8 +87,7 @@ namespace {
 
 constexpr int kBatchThreads = 256;
 
-// B loads of V values per lane: FP32 (V floats) or the BF16 copy (V bf16
-// values, half the bytes), widened to FP32.
+// B loads of V floats per lane (FP32 items).
 template <int V, bool BF16>
 struct RowLoad;
 template <int V>
@@ -106,29 +105,33 @@ struct RowLoad<V, false> {
         }
     }
 };
+// V bf16 values of the BF16 copy of B as raw words (value i in the low
+// (even i) or high (odd i) half of word i / 2).
 template <int V>
-struct RowLoad<V, true> {
-    static __device__ __forceinline__ void load(const BatchProb &p, int64_t off, float (&b)[V])
-    {
-        const uint16_t *q = p.Bbf + off;
-        if constexpr (V == 8) {
-            const uint4 t = __ldg(reinterpret_cast<const uint4 *>(q));
-            b[0] = __uint_as_float(t.x << 16); b[1] = __uint_as_float(t.x & 0xffff0000u);
-            b[2] = __uint_as_float(t.y << 16); b[3] = __uint_as_float(t.y & 0xffff0000u);
-            b[4] = __uint_as_float(t.z << 16); b[5] = __uint_as_float(t.z & 0xffff0000u);
-            b[6] = __uint_as_float(t.w << 16); b[7] = __uint_as_float(t.w & 0xffff0000u);
-        } else if constexpr (V == 4) {
-            const uint2 t = __ldg(reinterpret_cast<const uint2 *>(q));
-            b[0] = __uint_as_float(t.x << 16); b[1] = __uint_as_float(t.x & 0xffff0000u);
-            b[2] = __uint_as_float(t.y << 16); b[3] = __uint_as_float(t.y & 0xffff0000u);
-        } else if constexpr (V == 2) {
-            const uint32_t t = __ldg(reinterpret_cast<const unsigned int *>(q));
-            b[0] = __uint_as_float(t << 16); b[1] = __uint_as_float(t & 0xffff0000u);
-        } else {
-            b[0] = __uint_as_float(static_cast<uint32_t>(__ldg(reinterpret_cast<const unsigned short *>(q))) << 16);
-        }
+__device__ __forceinline__ void load_bf16_words(const uint16_t *q, uint32_t (&w)[(V + 1) / 2])
+{
+    if constexpr (V == 8) {
+        const uint4 t = __ldg(reinterpret_cast<const uint4 *>(q));
+        w[0] = t.x; w[1] = t.y; w[2] = t.z; w[3] = t.w;
+    } else if constexpr (V == 4) {
+        const uint2 t = __ldg(reinterpret_cast<const uint2 *>(q));
+        w[0] = t.x; w[1] = t.y;
+    } else if constexpr (V == 2) {
+        w[0] = __ldg(reinterpret_cast<const unsigned int *>(q));
+    } else {
+        w[0] = __ldg(reinterpret_cast<const unsigned short *>(q));
     }
-};
+}
+
+// acc + a * b with bf16 a and b and one rounding (the mixed-precision FMA of
+// sm_100+): a product of two bf16 values is exact in FP32, so this is fmaf on
+// the widened values, without widening b first.
+__device__ __forceinline__ float fma_bf16(uint16_t a, uint16_t b, float c)
+{
+    float d;
+    asm("fma.rn.f32.bf16 %0, %1, %2, %3;" : "=f"(d) : "h"(a), "h"(b), "f"(c));
+    return d;
+}
 
 template <int V>
 __device__ __forceinline__ void store_row(float *out, const float (&acc)[V])
@@ -167,33 +170,65 @@ __device__ __forceinline__ void item_rows(const BatchProb &p, int row0, int row1
             for (int v = 0; v < V; ++v)
                 acc[v] = 0.0f;
             int64_t e = e0;
+            if constexpr (BF16) {
+                // raw bf16 words of B and the mixed-precision FMA: the same
+                // results as widening both to FP32 and fmaf
 #pragma unroll 1
-            for (; e + 4 <= e1; e += 4) {
-                Entry t[4];
-                float b[4][V];
+                for (; e + 4 <= e1; e += 4) {
+                    Entry t[4];
+                    uint32_t w[4][(V + 1) / 2];
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    t[u] = p.packed[e + u];
+                    for (int u = 0; u < 4; ++u)
+                        t[u] = p.packed[e + u];
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    RowLoad<V, BF16>::load(p, static_cast<int64_t>(t[u].col) * p.n + j, b[u]);
+                    for (int u = 0; u < 4; ++u)
+                        load_bf16_words<V>(p.Bbf + static_cast<int64_t>(t[u].col) * p.n + j, w[u]);
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const float a = BF16 ? __bfloat162float(__float2bfloat16_rn(t[u].val)) : t[u].val;
+                    for (int u = 0; u < 4; ++u) {
+                        const __nv_bfloat16 ab = __float2bfloat16_rn(t[u].val);
+                        const uint16_t a = __bfloat16_as_ushort(ab);
+#pragma unroll
+                        for (int v = 0; v < V; ++v)
+                            acc[v] = fma_bf16(a, static_cast<uint16_t>((v & 1) ? (w[u][v >> 1] >> 16) : w[u][v >> 1]),
+                                              acc[v]);
+                    }
+                }
+#pragma unroll 1
+                for (; e < e1; ++e) {
+                    const Entry t = p.packed[e];
+                    uint32_t w[(V + 1) / 2];
+                    load_bf16_words<V>(p.Bbf + static_cast<int64_t>(t.col) * p.n + j, w);
+                    const uint16_t a = __bfloat16_as_ushort(__float2bfloat16_rn(t.val));
 #pragma unroll
                     for (int v = 0; v < V; ++v)
-                        acc[v] = fmaf(a, b[u][v], acc[v]);
+                        acc[v] = fma_bf16(a, static_cast<uint16_t>((v & 1) ? (w[v >> 1] >> 16) : w[v >> 1]), acc[v]);
                 }
-            }
+            } else {
 #pragma unroll 1
-            for (; e < e1; ++e) {
-                const Entry t = p.packed[e];
-                float b[V];
-                RowLoad<V, BF16>::load(p, static_cast<int64_t>(t.col) * p.n + j, b);
-                const float a = BF16 ? __bfloat162float(__float2bfloat16_rn(t.val)) : t.val;
+                for (; e + 4 <= e1; e += 4) {
+                    Entry t[4];
+                    float b[4][V];
 #pragma unroll
-                for (int v = 0; v < V; ++v)
-                    acc[v] = fmaf(a, b[v], acc[v]);
+                    for (int u = 0; u < 4; ++u)
+                        t[u] = p.packed[e + u];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        RowLoad<V, false>::load(p, static_cast<int64_t>(t[u].col) * p.n + j, b[u]);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+#pragma unroll
+                        for (int v = 0; v < V; ++v)
+                            acc[v] = fmaf(t[u].val, b[u][v], acc[v]);
+                }
+#pragma unroll 1
+                for (; e < e1; ++e) {
+                    const Entry t = p.packed[e];
+                    float b[V];
+                    RowLoad<V, false>::load(p, static_cast<int64_t>(t.col) * p.n + j, b);
+#pragma unroll
+                    for (int v = 0; v < V; ++v)
+                        acc[v] = fmaf(t.val, b[v], acc[v]);
+                }
             }
             store_row<V>(p.C + static_cast<int64_t>(row) * p.n + j, acc);
         }
