@@ -110,3 +110,43 @@ def test_irregular_zipf_rows(native, oracle_mod, torch):
     ref = oracle_mod.spdm(oracle_mod.convert(sub, 1), B.cpu().numpy())
     got = C[torch.from_numpy(pick).cuda()].cpu().numpy()
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+def test_batched_odd_widths_every_item_shape(native, torch):
+    """Widths that are not multiples of 4 or 8 (and unaligned C) take the
+    narrower item shapes -- 2 or 1 values per lane, 16 or 32 lanes per row --
+    in both forms: FP32 bit-identical to gcoo_spdm, BF16 to the FMA form."""
+    from gcoospdm_gb300 import datagen as dg
+    out = []
+    for i, (m, k, n) in enumerate([(77, 64, 1), (130, 96, 3), (64, 200, 6), (300, 128, 20), (91, 64, 40),
+                                   (257, 100, 100), (40, 64, 130)]):
+        A = dg.bernoulli_dense_torch(2000 + i, m, k, 0.1, device="cuda")
+        B = dg.dense_pm1_torch(2000 + i, 5, k, n, device="cuda")
+        out.append((native.GcooHandle(A).build(), A, B))
+    Cs = [torch.full((h.m, B.shape[1]), float("nan"), device="cuda") for h, A, B in out]
+    batch = native.GcooBatch([(h, B, C) for (h, A, B), C in zip(out, Cs)], prec="fp32")
+    batch.run()
+    torch.cuda.synchronize()
+    for (h, A, B), C in zip(out, Cs):
+        assert torch.equal(C, h.spdm(B))
+    # BF16 needs k * n % 4 == 0 (true for every k above)
+    Cb = [torch.full((h.m, B.shape[1]), float("nan"), device="cuda") for h, A, B in out]
+    batch = native.GcooBatch([(h, B, C) for (h, A, B), C in zip(out, Cb)], prec="bf16")
+    batch.run()
+    torch.cuda.synchronize()
+    for (h, A, B), C in zip(out, Cb):
+        ref = native.GcooHandle(A, engine="cuda_core").build()
+        n = B.shape[1]
+        if n % 8 == 0:  # the single-problem BF16 FMA form's width rule
+            assert torch.equal(C, ref.spdm(B, prec="bf16"))
+        Bq = B.to(torch.bfloat16).double()
+        Aq = A.to(torch.bfloat16).double()
+        exact = Aq @ Bq
+        assert float(torch.linalg.norm(C.double() - exact) / torch.linalg.norm(exact)) <= 1e-5
+
+
+def test_l2_read_peak_probe(native, torch):
+    """The roofline denominator bench.py measures live: an L2-resident gather
+    (512-byte warp loads) between 5 and 60 TB/s on a GB300."""
+    gbs = native.measure_l2_read_gbs()
+    assert 5000.0 < gbs < 60000.0, gbs
