@@ -171,7 +171,7 @@ gcoo_status spdm_fp32(gcoo_handle *h, const float *dB, int64_t n, float *dC, cud
                                       h->split_part.ptr, dC, h->side)
                   : launch_spdm_long(h->packed.ptr, h->row_ptr.ptr, h->long_rows.ptr, h->n_long, dB, n, dC, h->side);
         const cudaError_t es = el == cudaSuccess
-                                   ? launch_spdm_short(h->packed.ptr, h->row_ptr.ptr, h->m, dB, n, dC, long_row_min(), st)
+                                   ? launch_spdm_short(h->packed.ptr, h->row_ptr.ptr, h->m, h->k, dB, n, dC, long_row_min(), st)
                                    : cudaSuccess;
         // joined whatever happened: nothing of this call runs past it on the side stream
         GCOO_CUDA(cudaEventRecord(h->ev_join, h->side));

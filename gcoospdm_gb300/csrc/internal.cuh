@@ -169,9 +169,10 @@ cudaError_t launch_spdm_fp32(const Entry *packed, const int32_t *row_ptr, int64_
                              int64_t n, float *C, const LaunchShape &s, uint32_t *status,
                              cudaStream_t st);
 // The rows shorter than long_min, one warp per (row, column tile), nothing
-// staged (skewed matrices, whose long rows go to launch_spdm_long).
-cudaError_t launch_spdm_short(const Entry *packed, const int32_t *row_ptr, int64_t m, const float *B, int64_t n,
-                              float *C, int32_t long_min, cudaStream_t st);
+// staged (skewed matrices, whose long rows go to launch_spdm_long); k is
+// B's row count, which sets the walk order.
+cudaError_t launch_spdm_short(const Entry *packed, const int32_t *row_ptr, int64_t m, int64_t k, const float *B,
+                              int64_t n, float *C, int32_t long_min, cudaStream_t st);
 // ---- FP8-B scales (spdm_lowp.cu) -----------------------------------------------------------
 // scale[j] = the smallest power of two with absmax(B[:, j]) / scale[j] <= 448;
 // n % 4 == 0, B 16-byte aligned; amax: n words of scratch.

@@ -46,7 +46,7 @@ def zipf_case():
     return A, counts
 
 
-@pytest.mark.parametrize("n", [256, 200, 520])
+@pytest.mark.parametrize("n", [256, 200, 520, 1040])  # 1040: B of 34 MB, the short rows walk tile-major
 def test_split_sum_within_tolerance_and_short_rows_exact(native, oracle_mod, torch, zipf_case, n):
     from gcoospdm_gb300 import datagen as dg
     A, counts = zipf_case
