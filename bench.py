@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--sweep", action="store_true", help="print the FP32 n x sparsity sweep instead")
     ap.add_argument("--no-sweep", action="store_true", help="skip the sweep key of the main line")
     ap.add_argument("--case", choices=["tc_bf16", "tc_split", "convert", "fp32", "batched", "fp8", "bf16_fma",
-                                       "fp32_block", "convert_irregular", "spdm_irregular"],
+                                       "fp32_block", "convert_irregular", "spdm_irregular", "spdm_irregular_split"],
                     help="run one small case a few times (for profiling) and exit")
     return ap.parse_args()
 
@@ -81,12 +81,14 @@ def run_case(args):
         h = g.GcooHandle(A)
         print(json.dumps({"first_build_ms": round(_time(torch, h.build, reps=1, warm=0), 4),
                           "rebuild_ms": round(_time(torch, h.build, reps=3, warm=0), 4), "nnz": h.nnz}))
-    elif args.case == "spdm_irregular":
-        # the irregular workload's multiply, from COO input (no 17 GB dense operand)
+    elif args.case in ("spdm_irregular", "spdm_irregular_split"):
+        # the irregular workload's multiply, from COO input (no 17 GB dense operand);
+        # _split: the long rows summed in 32-entry pieces (gcoo_params.fp32_sum = split)
         m, n = 65536, 256
         rows, cols, vals = dg.zipf_coo(65536, m, m, 1_200_000, alpha=2.0, cap=4096)
         r32, c32 = torch.from_numpy(rows.astype("int32")).to(dev), torch.from_numpy(cols.astype("int32")).to(dev)
-        hc = g.GcooHandle.from_coo(r32, c32, torch.from_numpy(vals).to(dev), m=m, k=m).build()
+        mode = "split" if args.case == "spdm_irregular_split" else "chain"
+        hc = g.GcooHandle.from_coo(r32, c32, torch.from_numpy(vals).to(dev), m=m, k=m, fp32_sum=mode).build()
         B = torch.from_numpy(dg.normal_dense(65536, 40, m, n)).to(dev)
         Cd = torch.empty(m, n, device=dev)
         print(json.dumps({"spdm_ms": round(_time(torch, lambda: hc.spdm(B, Cd), reps=3, warm=1), 4)}))

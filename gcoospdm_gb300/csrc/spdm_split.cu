@@ -165,8 +165,19 @@ split_combine_kernel(const int32_t *__restrict__ row_ptr, const int32_t *__restr
     const int32_t pieces = (row_ptr[r + 1] - row_ptr[r] + kPiece - 1) / kPiece;
     const int32_t first = piece_first[li];
     const int32_t end = first + pieces < *total ? first + pieces : *total;
+    // eight partials' loads in flight at a time, added one by one in piece order
     float sum = 0.0f;
-    for (int32_t q = first; q < end; ++q)
+    int32_t q = first;
+    for (; q + 8 <= end; q += 8) {
+        float x[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            x[u] = part[static_cast<int64_t>(q + u) * n + j];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            sum += x[u];
+    }
+    for (; q < end; ++q)
         sum += part[static_cast<int64_t>(q) * n + j];
     C[static_cast<int64_t>(r) * n + j] = sum;
 }
