@@ -481,10 +481,17 @@ LaunchShape pick_shape(const gcoo_params &p, int64_t m, int64_t n, int64_t nnz, 
     if (v != 1 && v != 2 && v != 4)
         v = 1;
     s.vec = v;
-    const int cpg = s.rows;
     // Every group fits one staging chunk: one staging of a group's entries
-    // can serve several column tiles per warp.
-    const bool one_chunk = max_row > 0 && max_row * static_cast<int64_t>(s.rows) + 2 <= kChunk;
+    // can serve several column tiles per warp. With the launch shape left to
+    // the library, a CTA takes fewer rows (down to one) where that makes its
+    // group fit; rows of up to 2046 entries then stay on the one-warp-per-row
+    // path (any rows per CTA gives the same fmaf chains).
+    const auto fits = [&](int rows) { return max_row > 0 && max_row * static_cast<int64_t>(rows) + 2 <= kChunk; };
+    if (!skewed && p.warps <= 0 && p.col_warps <= 0)
+        while (s.rows > 1 && !fits(s.rows) && fits(1))
+            s.rows = s.rows / 2 > 0 ? s.rows / 2 : 1;
+    const int cpg = s.rows;
+    const bool one_chunk = fits(s.rows);
     int cw;
     if (p.col_warps > 0)
         cw = p.col_warps;

@@ -113,6 +113,21 @@ def test_heavy_group_multi_chunk(native, oracle_mod, torch):
     assert same_bits(h.spdm(dev(torch, B)).cpu().numpy(), ref)
 
 
+@pytest.mark.parametrize("density,n", [(0.06, 256), (0.12, 520), (0.3, 256)])
+def test_uniformly_long_rows(native, oracle_mod, torch, density, n):
+    """Rows of ~490, ~980 and ~2460 entries, not skewed: groups of four rows
+    overflow one staging chunk, so the launch takes two rows or one per CTA
+    (the first two) or stages in several passes (the last); the same bits
+    as the oracle's chain in every case."""
+    from gcoospdm_gb300 import datagen as dg
+    A = dg.bernoulli_dense(26, 600, 8192, density)
+    B = dg.dense_pm1(26, 5, 8192, n)
+    ref = oracle_mod.spdm(oracle_mod.convert(A), B)
+    h = native.GcooHandle(dev(torch, A)).build()
+    assert same_bits(h.spdm(dev(torch, B)).cpu().numpy(), ref)
+    assert h.device_status() == 0
+
+
 @pytest.mark.parametrize("n", [256, 200, 98, 36])
 def test_long_rows_of_skewed_matrices(native, oracle_mod, torch, n):
     """Skewed row lengths: rows of at least 256 entries go to the long-row
@@ -310,14 +325,15 @@ def test_multiply_by_on_changing_matrices(native, oracle_mod, torch):
 def test_width_beyond_grid_limit_is_refused(native, oracle_mod, torch):
     """Column tiles lie along the grid's y dimension: B wider than 65535
     tiles of the chosen shape is refused with GCOO_ERROR_CUDA before any
-    launch, and the handle stays usable. Groups of 4 rows of 600 entries
-    (more than one staging chunk) take one column tile per CTA (groups that
-    fit one chunk walk several, which widens the reach), n odd one column
-    per lane, two warps per row: 64-column tiles. B (10 GB) is never read."""
+    launch, and the handle stays usable. With the launch shape given (two
+    warps per row, which also keeps four rows per CTA), groups of 4 rows of
+    600 entries (more than one staging chunk) take one column tile per CTA
+    (groups that fit one chunk walk several, which widens the reach), n odd
+    one column per lane: 64-column tiles. B (10 GB) is never read."""
     from gcoospdm_gb300 import datagen as dg
-    native.autotune_clear()  # the default shape, not a tuned wider one
+    native.autotune_clear()  # the given shape, not a tuned wider one
     A = dg.bernoulli_dense(42, 8, 600, 1.0)
-    h = native.GcooHandle(dev(torch, A), fp32_order="rows").build()
+    h = native.GcooHandle(dev(torch, A), fp32_order="rows", col_warps=2).build()
     n = 65535 * 64 + 1
     wide = torch.empty(600, n, device="cuda")
     with pytest.raises(native.GcooError) as e:
