@@ -1,7 +1,7 @@
 // forms.cu -- dispatch of the reduced-precision forms (gcoo_spdm_ex) to an
 // engine: the tcgen05 tensor-core engine (spdm_tc.cu) where the matrix's
-// entries densify into 128 x 16 tiles, the FMA engine (spdm_lowp.cu)
-// elsewhere. FP8-B on the tensor engine: B quantized to E4M3 with
+// entries densify into 16-column tiles of its row panels (256 rows for BF16
+// and FP8-B, 128 for split-BF16), the FMA engine (spdm_lowp.cu) elsewhere. FP8-B on the tensor engine: B quantized to E4M3 with
 // power-of-two column scales and multiplied as exact BF16 values (kind::f16
 // needs both operands 16-bit), A in BF16 as for the BF16 form.
 #include "handle.hpp"
@@ -19,9 +19,9 @@ double tc_density(const gcoo_handle *h);
 gcoo_status tc_prepare_b(gcoo_handle *h, int64_t n, bool fp8);
 gcoo_status tc_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, bool fp8, cudaStream_t st);
 
-// Entries per stored tile slot above which the tensor engine wins: a 128 x 16
-// BF16 tile costs one MMA whatever its fill, which the tensor pipe runs at
-// more than 16x the rate the FMA pipes serve one entry per output column.
+// Entries per stored tile slot above which the tensor engine wins: a tile
+// costs its MMAs whatever its fill, which the tensor pipe runs at more than
+// 16x the rate the FMA pipes serve one entry per output column.
 constexpr double kTensorDensity = 1.0 / 16.0;
 
 bool form_uses_tensor(gcoo_handle *h, gcoo_precision prec)

@@ -2,41 +2,50 @@
 // densify into 16-wide blocks.
 //
 // Plan (built once per handle and form, from the GCOO entries):
-//   * A is cut into panels of 128 rows; a tile is the 128 x 16 slice of a
-//     panel at column block cb; a tile is active when it holds any entry;
-//   * each active tile is stored densely (zeros where A has none) as BF16 in
-//     the K-major, 32-byte-swizzled shared-memory layout of tcgen05 (row r at
-//     r*32 bytes, 16-byte chunk c at (c ^ ((r >> 2) & 1)) * 16), so one 4 KB
-//     bulk copy lands it ready for the MMA; split-BF16 keeps two more tiles
-//     (lo = x - hi and lo2 = x - hi - lo, each rounded to BF16: hi + lo +
-//     lo2 is x exactly), stored side by side;
+//   * A is cut into panels (256 rows for BF16 and FP8-B, 128 for split-BF16);
+//     a tile is the panel's 16-column slice at column block cb, active when
+//     it holds any entry;
+//   * each active tile is stored densely (zeros where A has none) as BF16,
+//     each 128-row half in the K-major, 32-byte-swizzled shared-memory layout
+//     of tcgen05 (row r at r*32 bytes, 16-byte chunk c at
+//     (c ^ ((r >> 2) & 1)) * 16), so a 4 KB copy lands a half ready for the
+//     MMA; split-BF16 keeps two more tiles (lo = x - hi and lo2 = x - hi -
+//     lo, each rounded to BF16: hi + lo + lo2 is x exactly), stored side by
+//     side;
 //   * B is converted per call into tiles of N output columns x 16 k (the
 //     same layout, N rows of 32 bytes).
-// Kernel: one CTA per (panel, N-column tile); warp 0 streams the panel's
-// active tiles through an S-stage ring of shared-memory slots with
-// cp.async.bulk on mbarriers, warp 1 issues one tcgen05.mma kind::f16
-// (M=128, N, K=16; six for split-BF16) per tile into an FP32 accumulator in
-// tensor memory, tcgen05.commit frees each slot, and all four warps drain the
-// accumulator with tcgen05.ld into C. Every wait is bounded.
+// BF16 / FP8-B kernel (spdm_tc_pair_kernel): a cluster of two CTAs on two
+// SMs per (256-row panel, 256 or 512 output columns); each CTA streams its
+// 128-row half of four tiles and its 128-column halves of their B tiles per
+// stage with tensor-map bulk copies (cta_group::2, completing on the first
+// CTA's barrier), and the first CTA issues tcgen05.mma.cta_group::2 (M=256,
+// N=256, K=16) into both CTAs' tensor memory, one accumulator per 256
+// columns. Split-BF16 kernel (spdm_tc_kernel): one CTA per (128-row panel,
+// 128 columns), one stage per tile, six MMAs per tile. Every wait is bounded.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
+
+#include <cuda.h>
+
+#include <mutex>
 
 #include "handle.hpp"
 
 namespace gcoo {
 
-constexpr int kPanel = 128;   // rows per tile (MMA M)
+constexpr int kPanel = 128;   // rows of a tile half (one CTA's MMA rows)
 constexpr int kTileK = 16;    // columns per tile (MMA K)
-constexpr int kTileBytes = kPanel * kTileK * 2;
+constexpr int kTileBytes = kPanel * kTileK * 2; // one 128-row half
 
 struct TcPlan {
     int64_t panels = 0, kb = 0, tiles = 0;
+    int panel_rows = kPanel; // 256 for the pair kernel (two halves per tile), 128 for split-BF16
     bool split = false;
     int64_t nnz = 0;
     DevBuf<int32_t> pf;       // exclusive prefix over (panel, cb) flags, size panels*kb + 1
     DevBuf<int32_t> tile_cb;  // cb of each tile (ascending within a panel)
-    DevBuf<uint16_t> a_hi;    // tiles * 2048 bf16 (swizzled)
+    DevBuf<uint16_t> a_hi;    // tiles * (panel_rows / 128) * 2048 bf16 (swizzled halves)
     DevBuf<uint16_t> a_lo;    // split only: tiles * 2 * 2048 bf16 (lo, then lo2, per tile)
     DevBuf<int64_t> scratch;
     // B workspace (per call)
@@ -45,6 +54,10 @@ struct TcPlan {
     // FP8-B: per-column power-of-two scales (and their absmax scratch)
     DevBuf<float> b_scale;
     DevBuf<unsigned> b_amax;
+    // tensor maps of the pair kernel's copies (host copies, passed by value)
+    CUtensorMap map_a, map_b;
+    const void *map_a_base = nullptr, *map_b_base = nullptr;
+    uint64_t map_a_rows = 0, map_b_rows = 0;
 };
 
 void destroy_tc_plan(TcPlan *p) { delete p; }
@@ -114,13 +127,13 @@ __host__ __device__ __forceinline__ uint32_t sw32_offset(uint32_t r, uint32_t c)
 
 // ---- plan building --------------------------------------------------------------------
 __global__ void tile_flags_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ row_ptr, int64_t m,
-                                  int64_t kb, int32_t *__restrict__ flags)
+                                  int64_t kb, int panel_rows, int32_t *__restrict__ flags)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     for (int64_t r = warp; r < m; r += nw) {
-        const int64_t base = (r / kPanel) * kb;
+        const int64_t base = (r / panel_rows) * kb;
         for (int64_t e = row_ptr[r] + lane; e < row_ptr[r + 1]; e += 32)
             flags[base + packed[e].col / kTileK] = 1;
     }
@@ -134,22 +147,25 @@ __global__ void tile_list_kernel(const int32_t *__restrict__ pf, int64_t total, 
             tile_cb[pf[f]] = static_cast<int32_t>(f % kb);
 }
 
+// lo (split-BF16 only) is filled with 128-row panels.
 __global__ void tile_fill_kernel(const Entry *__restrict__ packed, const int32_t *__restrict__ row_ptr, int64_t m,
-                                 int64_t kb, const int32_t *__restrict__ pf, __nv_bfloat16 *__restrict__ hi,
-                                 __nv_bfloat16 *__restrict__ lo)
+                                 int64_t kb, int panel_rows, const int32_t *__restrict__ pf,
+                                 __nv_bfloat16 *__restrict__ hi, __nv_bfloat16 *__restrict__ lo)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    const int64_t tile_elems = static_cast<int64_t>(panel_rows / kPanel) * (kTileBytes / 2);
     for (int64_t r = warp; r < m; r += nw) {
-        const int64_t base = (r / kPanel) * kb;
-        const uint32_t lr = static_cast<uint32_t>(r % kPanel);
+        const int64_t base = (r / panel_rows) * kb;
+        const uint32_t lr = static_cast<uint32_t>(r % panel_rows);
         for (int64_t e = row_ptr[r] + lane; e < row_ptr[r + 1]; e += 32) {
             const Entry t = packed[e];
             const int64_t tile = pf[base + t.col / kTileK];
-            const uint32_t off = sw32_offset(lr, static_cast<uint32_t>(t.col % kTileK)) / 2;
+            const uint32_t off = (lr / kPanel) * (kTileBytes / 2) +
+                                 sw32_offset(lr % kPanel, static_cast<uint32_t>(t.col % kTileK)) / 2;
             const __nv_bfloat16 h = __float2bfloat16_rn(t.val);
-            hi[tile * (kTileBytes / 2) + off] = h;
+            hi[tile * tile_elems + off] = h;
             if (lo) {
                 const float r1 = t.val - __bfloat162float(h); // exact
                 const __nv_bfloat16 l1 = __float2bfloat16_rn(r1);
@@ -398,11 +414,303 @@ spdm_tc_kernel(const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_
     }
 }
 
-// Output columns per CTA. A CTA's ring is sized (~98 KB) so that two CTAs
-// share an SM; split-BF16 keeps two accumulator banks, so it uses 128-column
-// tiles to stay within half of the 512 tensor-memory columns. (Four banks in
-// all 512 columns, one CTA per SM with a 12-stage ring, measured 1.8x slower.)
-int tile_n_for(int64_t n, bool split) { return (!split && n >= 256) ? 256 : 128; }
+// ---- the pair kernel (BF16, FP8-B) ----------------------------------------------------
+__device__ __forceinline__ uint32_t cluster_rank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// The shared::cluster address of `saddr` (a shared::cta address) in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t mapa_rank(uint32_t saddr, uint32_t rank)
+{
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+    return r;
+}
+
+__device__ __forceinline__ void cluster_sync_all()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// One box of a 2-D tensor map into this CTA's shared memory, completing on an
+// mbarrier in either CTA of the pair.
+__device__ __forceinline__ void tma_2d_pair(uint32_t dst, const CUtensorMap *map, int32_t x, int32_t y, uint32_t mbar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_mma_pair(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                 "l"(a), "l"(b), "r"(idesc), "r"(acc)
+                 : "memory");
+}
+
+// Arrives on the mbarrier at the same offset in both CTAs once the MMAs issued so far have completed.
+__device__ __forceinline__ void tc_commit_pair(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+                 ::"r"(smem_u32(bar)), "h"(static_cast<uint16_t>(3))
+                 : "memory");
+}
+
+constexpr int kPairN = 256;                // output columns per accumulator (MMA N)
+constexpr int kPairMaxNT = 2;              // accumulators per CTA: all 512 tensor-memory columns
+constexpr int kPairK = 4;                  // tiles per stage
+constexpr int kPairHalf = kTileBytes;      // 4 KB: a tile's 128-row half, or a B tile's 128-column half
+constexpr int kPairStage = (1 + kPairMaxNT) * kPairK * kPairHalf; // [A halves][B halves, accumulator 0][... 1]
+constexpr int kPairS = 4;                  // stages of 48 KB: 194 KB, so one CTA per SM
+constexpr int kPairSmem = 1024 + kPairS * kPairStage + 1024;
+constexpr uint64_t kPairDrainNs = 2000000; // after a wait gives up: time for copies in flight to land
+static_assert(kPairSmem <= 227 * 1024 && 2 * kPairSmem > 228 * 1024,
+              "one pair CTA per SM: its tensor-memory allocation never waits for another");
+
+// One cluster of two CTAs per (256-row panel, nt * 256 output columns). CTA
+// `rank` holds rows [128 rank, 128 rank + 128) of the panel: per stage its
+// halves of up to four of the panel's tiles and the matching 128-column
+// halves of the B tiles, copied by its warp 0 with tensor-map bulk copies
+// that complete on the first CTA's `full` barrier (which expects both CTAs'
+// bytes). Warp 1 of the first CTA issues, per tile and accumulator, one
+// tcgen05.mma.cta_group::2 (M=256, N=256, K=16) reading both CTAs' shared
+// memory, and tcgen05.commit frees the slot in both CTAs. Each CTA drains
+// its 128 rows of the accumulators from its own tensor memory.
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(128, 1)
+spdm_tc_pair_kernel(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
+                    const int32_t *__restrict__ pf, const int32_t *__restrict__ tile_cb, int64_t m, int64_t n,
+                    int64_t kb, int nt_cta, float *__restrict__ C, uint32_t *__restrict__ status)
+{
+    constexpr int N = kPairN, S = kPairS;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // the same carve in both CTAs: the MMA reads the second CTA's operands at the first's offsets
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+    uint64_t *full = reinterpret_cast<uint64_t *>(base);
+    uint64_t *empty = full + S;
+    uint64_t *done = empty + S;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    unsigned char *stages = base + 1024;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = cluster_rank();
+    const int64_t panel = blockIdx.x >> 1;
+    const int64_t jt = blockIdx.y; // nt_cta accumulators of 256 columns
+    const int64_t t0 = pf[panel * kb];
+    const int64_t ntiles = pf[(panel + 1) * kb] - t0;
+    const int64_t nstages = (ntiles + kPairK - 1) / kPairK;
+    const int64_t ntn = (n + N - 1) / N;
+    const int nt = static_cast<int>(ntn - jt * nt_cta < nt_cta ? ntn - jt * nt_cta : nt_cta);
+    bool gave_up = false;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        fence_mbar_init();
+    }
+    if (warp == 2) {
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kPairMaxNT * N)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    cluster_sync_all(); // both CTAs' barriers initialised and tensor memory allocated
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (ntiles > 0) {
+        if (warp == 0 && lane == 0) {
+            // producer (both CTAs)
+            for (int64_t i = 0; i < nstages; ++i) {
+                const int s = static_cast<int>(i % S);
+                if (i >= S && !mbar_wait(&empty[s], static_cast<uint32_t>(((i / S) - 1) & 1))) {
+                    atomicOr(status, kStatusWaitTimeout);
+                    gave_up = true;
+                    break;
+                }
+                const int64_t q0 = i * kPairK;
+                const int nq = ntiles - q0 < kPairK ? static_cast<int>(ntiles - q0) : kPairK;
+                if (rank == 0) // both CTAs' bytes
+                    mbar_arrive_expect_tx(&full[s], static_cast<uint32_t>(2 * (1 + nt) * nq * kPairHalf));
+                const uint32_t st = smem_u32(stages + static_cast<size_t>(s) * kPairStage);
+                const uint32_t leader_full = mapa_rank(smem_u32(&full[s]), 0);
+                for (int q = 0; q < nq; ++q) {
+                    const int64_t tile = t0 + q0 + q;
+                    const int64_t cb = tile_cb[tile];
+                    // maps in rows of 512 B: a tile is 16 rows, a half 8
+                    tma_2d_pair(st + q * kPairHalf, &tm_a, 0, static_cast<int32_t>(tile * 16 + rank * 8), leader_full);
+                    for (int t = 0; t < nt; ++t)
+                        tma_2d_pair(st + ((1 + t) * kPairK + q) * kPairHalf, &tm_b, 0,
+                                    static_cast<int32_t>(((jt * nt_cta + t) * kb + cb) * 16 + rank * 8), leader_full);
+                }
+            }
+        } else if (warp == 1 && lane == 0 && rank == 0) {
+            // MMA issuer (first CTA only)
+            const uint32_t idesc = idesc_bf16(2 * kPanel, N);
+            for (int64_t i = 0; i < nstages; ++i) {
+                const int s = static_cast<int>(i % S);
+                if (!mbar_wait(&full[s], static_cast<uint32_t>((i / S) & 1))) {
+                    atomicOr(status, kStatusWaitTimeout);
+                    gave_up = true;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t st = smem_u32(stages + static_cast<size_t>(s) * kPairStage);
+                const int64_t q0 = i * kPairK;
+                const int nq = ntiles - q0 < kPairK ? static_cast<int>(ntiles - q0) : kPairK;
+                for (int q = 0; q < nq; ++q)
+                    for (int t = 0; t < nt; ++t)
+                        tc_mma_pair(tmem + static_cast<uint32_t>(t * N), smem_desc_sw32(st + q * kPairHalf),
+                                    smem_desc_sw32(st + ((1 + t) * kPairK + q) * kPairHalf), idesc,
+                                    (i > 0 || q > 0) ? 1u : 0u);
+                tc_commit_pair(&empty[s]); // the slot is free in both CTAs once these MMAs have read it
+            }
+            tc_commit_pair(done); // arrives in both CTAs when every MMA issued above has completed
+        }
+        __syncwarp();
+        const bool ok = mbar_wait(done, 0);
+        if (!ok && lane == 0)
+            atomicOr(status, kStatusWaitTimeout);
+        tc_fence_after();
+        const int64_t row = panel * (2 * kPanel) + rank * kPanel + warp * 32 + lane;
+        if (__all_sync(0xffffffffu, ok ? 1 : 0)) {
+#pragma unroll 1
+            for (int c = 0; c < nt * N; c += 32) {
+                float v[32];
+                tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(c), v);
+                const int64_t j = jt * nt_cta * N + c;
+                if (row < m && j < n) {
+                    float *out = C + row * n + j;
+                    if (j + 32 <= n) {
+#pragma unroll
+                        for (int q = 0; q < 32; q += 4)
+                            *reinterpret_cast<float4 *>(out + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 32; ++q)
+                            if (j + q < n)
+                                out[q] = v[q];
+                    }
+                }
+            }
+        }
+    } else {
+        // panel without entries: its C rows are zero
+        const int64_t row = panel * (2 * kPanel) + rank * kPanel + warp * 32 + lane;
+        if (row < m)
+            for (int64_t j = jt * nt_cta * N; j < (jt + 1) * nt_cta * N && j < n; ++j)
+                C[row * n + j] = 0.0f;
+    }
+    // after a wait gave up (in either CTA: the status word), copies already
+    // issued may still be landing in this CTA or signalling the first CTA's
+    // barriers: give them a bounded time before the pair leaves
+    if (threadIdx.x == 0 && (gave_up || (*reinterpret_cast<volatile uint32_t *>(status) & kStatusWaitTimeout))) {
+        const uint64_t t_end = global_ns() + kPairDrainNs;
+        while (global_ns() < t_end)
+            __nanosleep(10000);
+    }
+    tc_fence_before();
+    cluster_sync_all(); // neither CTA leaves while the pair's MMAs or copies may touch it
+    if (warp == 2) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kPairMaxNT * N)
+                     : "memory");
+    }
+}
+
+// Columns of a B tile: 256 for the pair kernel, 128 for split-BF16, whose
+// two accumulator banks stay within half of the 512 tensor-memory columns so
+// that two of its CTAs (~98 KB rings) share an SM. (Four banks in all 512
+// columns, one CTA per SM with a 12-stage ring, measured 1.8x slower.)
+int tile_n_for(bool split) { return split ? 128 : kPairN; }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry-point query (no
+// driver library linked).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void *f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(f);
+    });
+    return fn;
+}
+
+// A buffer of swizzled tiles as a 2-D map of 512-byte rows (256 bf16),
+// boxes of 8 rows: one box is one contiguous 4 KB half. The bytes are
+// already in the MMA's shared-memory layout, so the copy is unswizzled.
+// `halves` counts the buffer's 4 KB halves.
+bool encode_halves_map(CUtensorMap *map, const void *base, uint64_t halves)
+{
+    EncodeTiledFn fn = encode_tiled_fn();
+    if (!fn || halves == 0)
+        return false;
+    const cuuint64_t dims[2] = {256, halves * 8};
+    const cuuint64_t strides[1] = {512};
+    const cuuint32_t box[2] = {256, 8};
+    const cuuint32_t elem_strides[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, elem_strides,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Accumulators per CTA: two (each A half then feeds two MMAs) unless one per
+// CTA still leaves the grid within one wave of one CTA per SM.
+int pair_accumulators(int64_t panels, int64_t ntn)
+{
+    const int64_t pairs = static_cast<int64_t>(device_sms()) / 2;
+    return panels * ntn <= pairs ? 1 : kPairMaxNT;
+}
+
+cudaError_t launch_pair(TcPlan &p, int64_t m, int64_t n, float *C, uint32_t *status, cudaStream_t st)
+{
+    const int64_t ntn = (n + kPairN - 1) / kPairN;
+    const uint64_t a_halves = static_cast<uint64_t>(p.tiles) * 2, b_halves = static_cast<uint64_t>(ntn * p.kb) * 2;
+    if (p.map_a_base != p.a_hi.ptr || p.map_a_rows != a_halves) {
+        if (!encode_halves_map(&p.map_a, p.a_hi.ptr, a_halves))
+            return cudaErrorInvalidValue;
+        p.map_a_base = p.a_hi.ptr;
+        p.map_a_rows = a_halves;
+    }
+    if (p.map_b_base != p.b_hi.ptr || p.map_b_rows != b_halves) {
+        if (!encode_halves_map(&p.map_b, p.b_hi.ptr, b_halves))
+            return cudaErrorInvalidValue;
+        p.map_b_base = p.b_hi.ptr;
+        p.map_b_rows = b_halves;
+    }
+    // y coordinates of the maps are int32
+    if (static_cast<int64_t>(a_halves * 8) > 0x7fffffffLL || static_cast<int64_t>(b_halves * 8) > 0x7fffffffLL)
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(spdm_tc_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPairSmem);
+    if (e != cudaSuccess)
+        return e;
+    const int nt_cta = pair_accumulators(p.panels, ntn);
+    const int64_t gy = (ntn + nt_cta - 1) / nt_cta;
+    if (2 * p.panels > 0x7fffffffLL || gy > 65535)
+        return cudaErrorInvalidConfiguration;
+    dim3 grid(static_cast<unsigned>(2 * p.panels), static_cast<unsigned>(gy));
+    spdm_tc_pair_kernel<<<grid, 128, kPairSmem, st>>>(p.map_a, p.map_b, p.pf.ptr, p.tile_cb.ptr, m, n, p.kb, nt_cta, C,
+                                                      status);
+    count_launches(1);
+    return cudaGetLastError();
+}
 
 template <int N, int S, bool SPLIT>
 cudaError_t launch_tc(const TcPlan &p, int64_t m, int64_t n, float *C, uint32_t *status, cudaStream_t st)
@@ -425,7 +733,7 @@ cudaError_t launch_tc(const TcPlan &p, int64_t m, int64_t n, float *C, uint32_t 
 gcoo_status tc_build_plan(gcoo_handle *h, bool split, cudaStream_t st)
 {
     if (h->tc && h->tc->split == split && h->tc->nnz == h->nnz)
-        return GCOO_SUCCESS;
+        return GCOO_SUCCESS; // the same entries: built for this form already
     destroy_tc_plan(h->tc);
     h->tc = new (std::nothrow) TcPlan();
     if (!h->tc)
@@ -433,7 +741,8 @@ gcoo_status tc_build_plan(gcoo_handle *h, bool split, cudaStream_t st)
     TcPlan &p = *h->tc;
     p.split = split;
     p.nnz = h->nnz;
-    p.panels = (h->m + kPanel - 1) / kPanel;
+    p.panel_rows = split ? kPanel : 2 * kPanel;
+    p.panels = (h->m + p.panel_rows - 1) / p.panel_rows;
     p.kb = (h->k + kTileK - 1) / kTileK;
     const int64_t L = p.panels * p.kb;
     const size_t sc = scan_scratch_elems(L);
@@ -441,7 +750,7 @@ gcoo_status tc_build_plan(gcoo_handle *h, bool split, cudaStream_t st)
         return fail(GCOO_ERROR_ALLOC, "device allocation of the tile plan failed");
     GCOO_CUDA(cudaMemsetAsync(p.pf.ptr, 0, sizeof(int32_t) * (L + 1), st));
     unsigned blocks = static_cast<unsigned>(std::min<int64_t>((h->m + 7) / 8, 152 * 16));
-    tile_flags_kernel<<<blocks, 256, 0, st>>>(h->packed.ptr, h->row_ptr.ptr, h->m, p.kb, p.pf.ptr);
+    tile_flags_kernel<<<blocks, 256, 0, st>>>(h->packed.ptr, h->row_ptr.ptr, h->m, p.kb, p.panel_rows, p.pf.ptr);
     count_launches(1);
     GCOO_LAUNCH("tile_flags_kernel");
     GCOO_CUDA(launch_row_scan(p.pf.ptr, L, 1, nullptr, nullptr, p.scratch.ptr + sc, p.scratch.ptr, nullptr, st));
@@ -449,17 +758,17 @@ gcoo_status tc_build_plan(gcoo_handle *h, bool split, cudaStream_t st)
     GCOO_CUDA(cudaMemcpyAsync(&total, p.scratch.ptr + sc, sizeof(total), cudaMemcpyDeviceToHost, st));
     GCOO_CUDA(cudaStreamSynchronize(st));
     p.tiles = total;
-    const size_t tile_elems = static_cast<size_t>(kTileBytes / 2);
+    const size_t tile_elems = static_cast<size_t>(p.panel_rows / kPanel) * (kTileBytes / 2);
     if (!p.tile_cb.ensure(total + 1) || !p.a_hi.ensure(total * tile_elems + 1) ||
         (split && !p.a_lo.ensure(2 * total * tile_elems + 1)))
         return fail(GCOO_ERROR_ALLOC, "device allocation of the dense tiles failed");
     if (total > 0) {
         tile_list_kernel<<<static_cast<unsigned>(std::min<int64_t>((L + 255) / 256, 4096)), 256, 0, st>>>(p.pf.ptr, L,
                                                                                                           p.kb, p.tile_cb.ptr);
-        GCOO_CUDA(cudaMemsetAsync(p.a_hi.ptr, 0, total * kTileBytes, st));
+        GCOO_CUDA(cudaMemsetAsync(p.a_hi.ptr, 0, total * tile_elems * 2, st));
         if (split)
             GCOO_CUDA(cudaMemsetAsync(p.a_lo.ptr, 0, 2 * total * kTileBytes, st));
-        tile_fill_kernel<<<blocks, 256, 0, st>>>(h->packed.ptr, h->row_ptr.ptr, h->m, p.kb, p.pf.ptr,
+        tile_fill_kernel<<<blocks, 256, 0, st>>>(h->packed.ptr, h->row_ptr.ptr, h->m, p.kb, p.panel_rows, p.pf.ptr,
                                                  reinterpret_cast<__nv_bfloat16 *>(p.a_hi.ptr),
                                                  split ? reinterpret_cast<__nv_bfloat16 *>(p.a_lo.ptr) : nullptr);
         count_launches(2);
@@ -473,13 +782,13 @@ double tc_density(const gcoo_handle *h)
 {
     if (!h->tc || h->tc->tiles == 0)
         return 0.0;
-    return static_cast<double>(h->nnz) / (static_cast<double>(h->tc->tiles) * kPanel * kTileK);
+    return static_cast<double>(h->nnz) / (static_cast<double>(h->tc->tiles) * h->tc->panel_rows * kTileK);
 }
 
 gcoo_status tc_prepare_b(gcoo_handle *h, int64_t n, bool fp8)
 {
     TcPlan &p = *h->tc;
-    const int N = tile_n_for(n, p.split);
+    const int N = tile_n_for(p.split);
     const int64_t nt = (n + N - 1) / N;
     const size_t elems = static_cast<size_t>(nt) * p.kb * N * kTileK;
     if (!p.b_hi.ensure(elems) || (p.split && !p.b_lo.ensure(2 * elems)) ||
@@ -492,7 +801,7 @@ gcoo_status tc_prepare_b(gcoo_handle *h, int64_t n, bool fp8)
 gcoo_status tc_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, bool fp8, cudaStream_t st)
 {
     TcPlan &p = *h->tc;
-    const int N = tile_n_for(n, p.split);
+    const int N = tile_n_for(p.split);
     if (fp8)
         GCOO_CUDA(launch_fp8_scales(dB, h->k, n, p.b_amax.ptr, p.b_scale.ptr, st));
     dim3 g(static_cast<unsigned>(p.kb), static_cast<unsigned>((n + N - 1) / N));
@@ -501,15 +810,15 @@ gcoo_status tc_spdm(gcoo_handle *h, const float *dB, int64_t n, float *dC, bool 
                                       fp8 ? p.b_scale.ptr : nullptr);
     count_launches(1);
     GCOO_LAUNCH("b_tiles_kernel");
-    cudaError_t e;
-    if (N == 256)
-        e = launch_tc<256, 8, false>(p, h->m, n, dC, h->status.ptr, st);
-    else if (N == 128 && !p.split)
-        e = launch_tc<128, 12, false>(p, h->m, n, dC, h->status.ptr, st);
-    else
-        e = launch_tc<128, 4, true>(p, h->m, n, dC, h->status.ptr, st);
+    if (p.split) {
+        const cudaError_t e = launch_tc<128, 4, true>(p, h->m, n, dC, h->status.ptr, st);
+        if (e != cudaSuccess)
+            return cuda_fail(e, "spdm_tc_kernel launch");
+        return GCOO_SUCCESS;
+    }
+    const cudaError_t e = launch_pair(p, h->m, n, dC, h->status.ptr, st);
     if (e != cudaSuccess)
-        return cuda_fail(e, "spdm_tc_kernel launch");
+        return cuda_fail(e, "spdm_tc_pair_kernel launch (or its tensor maps)");
     return GCOO_SUCCESS;
 }
 
