@@ -204,6 +204,10 @@ b_tiles_kernel(const float *__restrict__ B, int64_t k, int64_t n, int N, int64_t
         float sc = 1.0f;
         if (fp8_scale && j < n)
             sc = fp8_scale[j];
+        // a power of two in the normal range has an exact reciprocal, so
+        // v * inv is v / sc exactly; otherwise divide
+        const bool by_inv = sc >= 1.17549435e-38f && sc <= 8.50705917e37f;
+        const float inv = by_inv ? 1.0f / sc : 0.0f;
         uint32_t wh[4], wl[4], wl2[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -213,7 +217,8 @@ b_tiles_kernel(const float *__restrict__ B, int64_t k, int64_t n, int N, int64_t
                 const int64_t c = cb * kTileK + half * 8 + q * 2 + e;
                 float v = (c < k && j < n) ? __ldg(B + c * n + j) : 0.0f;
                 if (fp8_scale && j < n) {
-                    const __nv_fp8_storage_t f8 = __nv_cvt_float_to_fp8(v / sc, __NV_SATFINITE, __NV_E4M3);
+                    const __nv_fp8_storage_t f8 =
+                        __nv_cvt_float_to_fp8(by_inv ? v * inv : v / sc, __NV_SATFINITE, __NV_E4M3);
                     v = __half2float(__half(__nv_cvt_fp8_to_halfraw(f8, __NV_E4M3))) * sc;
                 }
                 h2[e] = __float2bfloat16_rn(v);
