@@ -80,3 +80,31 @@ def test_tensor_engine_at_precision_form_size(native, torch, operands, s):
     assert errs["bf16_vs_exact"] <= 1e-2
     assert errs["split_vs_exact"] <= 5e-6
     assert errs["fp8_vs_quantized"] <= 1e-5
+
+
+def test_tensor_engine_ragged_panels_and_columns(native, torch):
+    """m = 8000 (the last 256-row panel partly filled) and n = 528 (two full
+    256-column accumulators and a 16-column one): two accumulators per CTA
+    (32 panels x 3 column tiles exceed one wave of one-accumulator pairs),
+    the second cluster column with one accumulator, masked to n. BF16 and
+    FP8-B on sampled rows, the last panel's rows included, against FP64 of
+    the rounded / quantized operands."""
+    from gcoospdm_gb300 import datagen as dg
+    m, k, n = 8000, 8192, 528
+    A = dg.block_dense_torch(9300, m, k, 0.25, device="cuda")
+    B = dg.dense_pm1_torch(9301, 5, k, n, device="cuda")
+    rows = list(range(3, m, 125)) + [m - 1]
+    idx = torch.tensor(rows, device="cuda")
+    h = native.GcooHandle(A, engine="tensor").build()
+    C = torch.empty(m, n, device="cuda")
+    h.spdm(B, C, prec="bf16")
+    assert h.query_engine("bf16")
+    err = rel_fro_t(torch, C[idx], bf16_round_t(torch, A[idx]) @ bf16_round_t(torch, B))
+    h.spdm(B, C, prec="fp8_b")
+    Bh = B.cpu().numpy()
+    sc = fp8_scales(Bh)
+    Bq = torch.from_numpy(e4m3_round(Bh / sc) * sc).cuda().double()
+    err8 = rel_fro_t(torch, C[idx], bf16_round_t(torch, A[idx]) @ Bq)
+    print(f"ragged: bf16 {err:.3e}, fp8_b {err8:.3e}")
+    assert h.device_status() == 0
+    assert err <= 1e-5 and err8 <= 1e-5
