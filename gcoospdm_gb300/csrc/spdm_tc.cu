@@ -468,10 +468,10 @@ __device__ __forceinline__ void tc_commit_pair(uint64_t *bar)
 
 constexpr int kPairN = 256;                // output columns per accumulator (MMA N)
 constexpr int kPairMaxNT = 2;              // accumulators per CTA: all 512 tensor-memory columns
-constexpr int kPairK = 4;                  // tiles per stage
+constexpr int kPairK = 8;                  // tiles per stage (4 x 4 stages: 3 % slower; 2 x 8: 12 %)
 constexpr int kPairHalf = kTileBytes;      // 4 KB: a tile's 128-row half, or a B tile's 128-column half
 constexpr int kPairStage = (1 + kPairMaxNT) * kPairK * kPairHalf; // [A halves][B halves, accumulator 0][... 1]
-constexpr int kPairS = 4;                  // stages of 48 KB: 194 KB, so one CTA per SM
+constexpr int kPairS = 2;                  // stages of 96 KB: 194 KB, so one CTA per SM
 constexpr int kPairSmem = 1024 + kPairS * kPairStage + 1024;
 constexpr uint64_t kPairDrainNs = 2000000; // after a wait gives up: time for copies in flight to land
 static_assert(kPairSmem <= 227 * 1024 && 2 * kPairSmem > 228 * 1024,
@@ -479,7 +479,7 @@ static_assert(kPairSmem <= 227 * 1024 && 2 * kPairSmem > 228 * 1024,
 
 // One cluster of two CTAs per (256-row panel, nt * 256 output columns). CTA
 // `rank` holds rows [128 rank, 128 rank + 128) of the panel: per stage its
-// halves of up to four of the panel's tiles and the matching 128-column
+// halves of up to kPairK of the panel's tiles and the matching 128-column
 // halves of the B tiles, copied by its warp 0 with tensor-map bulk copies
 // that complete on the first CTA's `full` barrier (which expects both CTAs'
 // bytes). Warp 1 of the first CTA issues, per tile and accumulator, one
