@@ -180,26 +180,42 @@ __global__ void tile_fill_kernel(const Entry *__restrict__ packed, const int32_t
 // With fp8_scale (FP8-B): each value is first quantized to E4M3 in units of
 // its column's power-of-two scale, then stored as the exact BF16 value of
 // E4M3 x scale, so the BF16 MMA multiplies the FP8-B operand exactly.
-// Each pair of lanes builds one 32-byte tile row (output column j): lane
-// half h converts B[cb*16 + 8h .. + 8][j] and stores them as one 16-byte
-// chunk, so a warp writes 16 whole rows (no partial-sector stores) while
-// its loads read 16 consecutive columns of two B rows at a time.
+// One CTA per tile: the 16 x N block of B is staged in shared memory with
+// coalesced 16-byte loads (64 lanes per 256 columns of a row), then thread
+// jj builds tile row jj (output column jt*N + jj: 16 values read down a
+// shared-memory column, conflict-free across the warp) and writes its 32
+// bytes with two 16-byte stores, so a warp writes 1 KB contiguous. (Lanes
+// loading 4-byte values down B's columns directly: 20 us for B 8192 x 1024.)
 __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo_half, __nv_bfloat16 hi_half)
 {
     return static_cast<uint32_t>(__bfloat16_as_ushort(lo_half)) |
            (static_cast<uint32_t>(__bfloat16_as_ushort(hi_half)) << 16);
 }
 
+constexpr int kBTileMaxN = 256;
+
+// Needs n % 4 == 0 and B 16-byte aligned (the tensor engine takes n % 16 == 0).
 __global__ void __launch_bounds__(256)
 b_tiles_kernel(const float *__restrict__ B, int64_t k, int64_t n, int N, int64_t kb, __nv_bfloat16 *__restrict__ hi,
                __nv_bfloat16 *__restrict__ lo, const float *__restrict__ fp8_scale)
 {
+    __shared__ __align__(16) float blk[kTileK][kBTileMaxN];
     const int64_t cb = blockIdx.x;
     const int64_t jt = blockIdx.y;
     const int64_t tile = jt * kb + cb;
     const size_t tile_elems = static_cast<size_t>(N) * kTileK;
-    const int half = threadIdx.x & 1;
-    for (int jj = threadIdx.x >> 1; jj < N; jj += blockDim.x >> 1) {
+    const int n4 = N / 4; // float4 columns per block row
+    for (int i = threadIdx.x; i < kTileK * n4; i += blockDim.x) {
+        const int r = i / n4, c4 = i - r * n4;
+        const int64_t c = cb * kTileK + r;
+        const int64_t j = jt * N + c4 * 4;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (c < k && j < n)
+            v = __ldg(reinterpret_cast<const float4 *>(B + c * n + j));
+        *reinterpret_cast<float4 *>(&blk[r][c4 * 4]) = v;
+    }
+    __syncthreads();
+    for (int jj = threadIdx.x; jj < N; jj += blockDim.x) {
         const int64_t j = jt * N + jj;
         float sc = 1.0f;
         if (fp8_scale && j < n)
@@ -208,14 +224,13 @@ b_tiles_kernel(const float *__restrict__ B, int64_t k, int64_t n, int N, int64_t
         // v * inv is v / sc exactly; otherwise divide
         const bool by_inv = sc >= 1.17549435e-38f && sc <= 8.50705917e37f;
         const float inv = by_inv ? 1.0f / sc : 0.0f;
-        uint32_t wh[4], wl[4], wl2[4];
+        uint32_t wh[8], wl[8], wl2[8];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < 8; ++q) {
             __nv_bfloat16 h2[2], l2[2], m2[2];
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
-                const int64_t c = cb * kTileK + half * 8 + q * 2 + e;
-                float v = (c < k && j < n) ? __ldg(B + c * n + j) : 0.0f;
+                float v = blk[q * 2 + e][jj];
                 if (fp8_scale && j < n) {
                     const __nv_fp8_storage_t f8 =
                         __nv_cvt_float_to_fp8(by_inv ? v * inv : v / sc, __NV_SATFINITE, __NV_E4M3);
@@ -230,12 +245,17 @@ b_tiles_kernel(const float *__restrict__ B, int64_t k, int64_t n, int N, int64_t
             wl[q] = pack_bf16(l2[0], l2[1]);
             wl2[q] = pack_bf16(m2[0], m2[1]);
         }
-        const uint32_t off = sw32_offset(static_cast<uint32_t>(jj), static_cast<uint32_t>(half * 8)) / 2;
-        *reinterpret_cast<uint4 *>(hi + tile * tile_elems + off) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
-        if (lo) {
-            *reinterpret_cast<uint4 *>(lo + 2 * tile * tile_elems + off) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
-            *reinterpret_cast<uint4 *>(lo + (2 * tile + 1) * tile_elems + off) =
-                make_uint4(wl2[0], wl2[1], wl2[2], wl2[3]);
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const uint32_t off = sw32_offset(static_cast<uint32_t>(jj), static_cast<uint32_t>(half * 8)) / 2;
+            const int w0 = half * 4;
+            *reinterpret_cast<uint4 *>(hi + tile * tile_elems + off) = make_uint4(wh[w0], wh[w0 + 1], wh[w0 + 2], wh[w0 + 3]);
+            if (lo) {
+                *reinterpret_cast<uint4 *>(lo + 2 * tile * tile_elems + off) =
+                    make_uint4(wl[w0], wl[w0 + 1], wl[w0 + 2], wl[w0 + 3]);
+                *reinterpret_cast<uint4 *>(lo + (2 * tile + 1) * tile_elems + off) =
+                    make_uint4(wl2[w0], wl2[w0 + 1], wl2[w0 + 2], wl2[w0 + 3]);
+            }
         }
     }
 }
